@@ -1,0 +1,154 @@
+/*
+ * skycube_gb300.h -- C ABI of the GB300 skycube engine.
+ *
+ * A skycube is the skyline of every non-empty subspace ("cuboid") S of an
+ * n x d float32 point set, smaller being better on every attribute. Point q
+ * dominates p on S iff q[k] <= p[k] for all k in S and q[k] < p[k] for some
+ * k in S; q strictly dominates p iff q[k] < p[k] for all k in S. The skyline
+ * of S holds the points nobody dominates on S; the extended skyline holds the
+ * dominated points nobody strictly dominates. Point ids are row indices of
+ * the input, cuboid ids are bitmasks (bit k = attribute k).
+ *
+ * The entry points replace the suite's single-GPU MDMC and SDSC paths:
+ *   skc_dataset_upload  -> MDMC<D>::Init / SDSC<D>::Init
+ *                          (src/mdmc/MDMC.cu:183-236, src/sdsc/SDSC.cu:28-58)
+ *                          plus initializeGpu's H2D copy
+ *                          (src/mdmc/MDMC.cu:1060-1084, src/sdsc/SDSC.cu:208-227)
+ *   skc_skycube         -> MDMC<D>::Execute (src/mdmc/MDMC.cu:524-616) and
+ *                          SDSC<D>::Execute (src/sdsc/SDSC.cu:248-335), with
+ *                          run_skyalign (src/sdsc/skyAlign.cu:9-53) inside
+ *   skc_result_cuboid   -> lattice_node::skyline of SDSC<D>::getLattice
+ *                          (src/sdsc/SDSC.h:39, src/utilities/
+ *                          lattice_utilities.h:21-31) and getsubspace over
+ *                          MDMC<D>::getHashCubeStructure (src/mdmc/MDMC.h:62,
+ *                          src/utilities/utilities.h:253-267)
+ *   skc_result_extended -> lattice_node::extended_sky
+ *   skc_result_bitmaps  -> the per-point dominated-subspace bitmaps that
+ *                          feed HashCube<D>::populateFromSingleNodeAux
+ *                          (src/skycube/Hashcube.h:107-115)
+ *
+ * Conventions: every call returns an int status (SKC_OK == 0) and never
+ * exits the process; skc_last_error() gives a one-line message for the
+ * calling thread. Objects created from one context must be used from one
+ * host thread at a time.
+ */
+#ifndef SKYCUBE_GB300_H_
+#define SKYCUBE_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define SKC_OK 0
+#define SKC_ERR_INVALID 1     /* bad argument: d out of range, NULL, non-finite value */
+#define SKC_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define SKC_ERR_OOM 3         /* device or host allocation failed */
+#define SKC_ERR_TIMEOUT 4     /* a device-side wait ran out of iterations */
+#define SKC_ERR_UNSUPPORTED 5 /* request outside what this build supports */
+#define SKC_ERR_REJECTED 6    /* admission refused the request (memory budget) */
+
+/* Limits. */
+#define SKC_MIN_DIMS 2
+#define SKC_MAX_DIMS 16
+
+/* Algorithms (the suite's -s values "mdmc" and "sdsc"). Both return the
+ * per-cuboid skylines; MDMC also exposes per-point bitmaps, SDSC also
+ * exposes per-cuboid extended skylines. */
+#define SKC_ALGO_MDMC 0
+#define SKC_ALGO_SDSC 1
+
+/* Execution forms. PLAIN issues one launch sequence per cuboid with a host
+ * round trip after each (the suite's SDSC shape; for MDMC, one bitmap launch
+ * per batch of points as in tombstoning_hearting_gpu). BATCHED computes all
+ * cuboids in one persistent launch with no host synchronisation until the
+ * result is read. */
+#define SKC_MODE_PLAIN 0
+#define SKC_MODE_BATCHED 1
+
+typedef struct skc_context skc_context;
+typedef struct skc_dataset skc_dataset;
+typedef struct skc_result skc_result;
+
+typedef struct skc_options {
+  int algo;        /* SKC_ALGO_* */
+  int mode;        /* SKC_MODE_* */
+  int max_d;       /* only cuboids with <= max_d attributes (-m); <= 0: all */
+  int depth;       /* grid depth: 2^depth cells per attribute, 1..7; 0: auto (-d) */
+  int want_extended; /* also produce per-cuboid extended skylines */
+  int want_bitmaps;  /* keep per-point bitmaps for skc_result_bitmaps */
+} skc_options;
+
+/* Fills *opt with defaults: MDMC, BATCHED, all cuboids, auto depth. */
+void skc_options_init(skc_options* opt);
+
+/* Creates a context on CUDA device `device` (the -g value). */
+int skc_context_create(int device, skc_context** out);
+int skc_context_destroy(skc_context* ctx);
+
+/* Copies n x d row-major float32 points from HOST memory to the device and
+ * keeps them resident. Rejects d outside [2,16], n == 0 and non-finite
+ * values. The caller keeps ownership of `rows`. */
+int skc_dataset_upload(skc_context* ctx, const float* rows, uint64_t n, int d,
+                       skc_dataset** out);
+/* Same, from a DEVICE pointer on the context's device (no host copy). */
+int skc_dataset_upload_device(skc_context* ctx, const float* d_rows,
+                              uint64_t n, int d, skc_dataset** out);
+int skc_dataset_free(skc_dataset* ds);
+
+/* Computes the skycube of `ds`. Results stay on the device until a
+ * skc_result_* accessor asks for host data. */
+int skc_skycube(skc_context* ctx, skc_dataset* ds, const skc_options* opt,
+                skc_result** out);
+
+/* Number of attributes of the result's dataset and number of candidate
+ * points (full-space skyline plus extended skyline). */
+int skc_result_info(skc_result* res, int* d, uint64_t* n_candidates,
+                    uint64_t* total_skyline_ids);
+
+/* Host view of one cuboid's skyline ids (ascending). The pointer stays valid
+ * until skc_result_free. Cuboids above max_d report count 0. */
+int skc_result_cuboid(skc_result* res, uint32_t cuboid, const uint32_t** ids,
+                      uint64_t* count);
+/* Host view of one cuboid's extended skyline ids (needs want_extended). */
+int skc_result_extended(skc_result* res, uint32_t cuboid,
+                        const uint32_t** ids, uint64_t* count);
+/* Device view of all skylines: ids of cuboid c are d_ids[d_offsets[c] ..
+ * d_offsets[c+1]); offsets has 2^d + 1 entries. */
+int skc_result_device_csr(skc_result* res, const uint64_t** d_offsets,
+                          const uint32_t** d_ids);
+/* Copies every cuboid's skyline to host memory in one go (CSR layout as
+ * above); afterwards skc_result_cuboid is a pure host lookup. */
+int skc_result_download(skc_result* res);
+/* Host copy of the per-point dominated-subspace bitmaps (needs
+ * want_bitmaps): point pids[i]'s bitmap is bits[i*words .. (i+1)*words),
+ * bit (s % 32) of word s / 32 set iff the point is dominated in cuboid s.
+ * words = max(1, 2^d / 32). */
+int skc_result_bitmaps(skc_result* res, const uint32_t** bits,
+                       const uint32_t** pids, uint64_t* n_points,
+                       uint32_t* words);
+int skc_result_free(skc_result* res);
+
+/* Milliseconds of device time of the last skc_skycube on this context,
+ * measured with CUDA events on the context's stream. */
+int skc_last_device_ms(skc_context* ctx, float* ms);
+
+/* Device time of one phase of the last skc_skycube on this context (CUDA
+ * events on the context's stream): index 0, 1, ... until SKC_ERR_INVALID.
+ * Phase names are stable strings such as "bitmap kernel". */
+int skc_last_phase(skc_context* ctx, int index, const char** name, float* ms);
+
+/* Number of kernels this library has launched in this process so far (all
+ * contexts). A caller brackets a region with two reads to count launches. */
+uint64_t skc_kernel_launches(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* skc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SKYCUBE_GB300_H_ */

@@ -1,0 +1,804 @@
+// C ABI of the skycube engine (include/skycube_gb300.h) and the host-side
+// orchestration of the device pipelines.
+//
+// Pipelines (all on the context's stream, device memory from the stream-
+// ordered pool):
+//
+//  full space   grid pivots + cells of all points, Manhattan-norm bucket
+//               order, skyline kernel on the full space, compaction into the
+//               full-space skyline, extended skyline and their union, the
+//               candidate set (ascending ids). Replaces gpu_extended_skyline
+//               + run_skyalign (src/mdmc/MDMC.cu:504-522).
+//
+//  BATCHED      candidate SoA copy, grid cells over the candidates, q order
+//               by median-mask lattice level, block minima, ONE persistent
+//               bitmap launch covering every cuboid, then device compaction
+//               of the bitmaps into per-cuboid id lists. No host round trip
+//               between the candidate count and the final size read.
+//
+//  PLAIN/SDSC   the suite's per-cuboid schedule (SDSC<D>::Execute,
+//               src/sdsc/SDSC.cu:248-335): lattice levels top-down, each
+//               cuboid's candidates are the skyline + extended skyline of its
+//               smallest computed parent (findMinParent, :366-376; full space
+//               when the first parent was skipped by max_d, :84-93); one
+//               launch sequence and one host synchronisation per cuboid.
+//
+//  PLAIN/MDMC   the bitmap kernel launched on batches of 5,600 points with a
+//               synchronisation after each batch, the shape of
+//               tombstoning_hearting_gpu (src/mdmc/MDMC.cu:752-857).
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdlib>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace skc {
+
+static thread_local std::string g_err;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+void clear_error() { g_err.clear(); }
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// Per-phase device timing: CUDA events on the context's stream, kept on the
+// context (skc_last_phase) and printed to stderr when SKC_TRACE=1.
+struct Tracer {
+  skc_context* ctx;
+  bool print;
+  std::vector<std::pair<const char*, cudaEvent_t>> marks;
+  explicit Tracer(skc_context* c) : ctx(c) {
+    const char* e = getenv("SKC_TRACE");
+    print = e && *e && *e != '0';
+    mark("start");
+  }
+  void mark(const char* name) {
+    cudaEvent_t ev;
+    if (cudaEventCreate(&ev) != cudaSuccess) return;
+    cudaEventRecord(ev, ctx->stream);
+    marks.push_back({name, ev});
+  }
+  ~Tracer() {
+    ctx->phases.clear();
+    if (!marks.empty() && cudaEventSynchronize(marks.back().second) == cudaSuccess) {
+      for (size_t i = 1; i < marks.size(); ++i) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, marks[i - 1].second, marks[i].second);
+        ctx->phases.push_back({marks[i].first, ms});
+        if (print) fprintf(stderr, "[skc] %-24s %9.3f ms\n", marks[i].first, ms);
+      }
+    }
+    for (auto& m : marks) cudaEventDestroy(m.second);
+  }
+};
+
+// Owns the temporary device buffers of one call; frees them stream-ordered.
+struct Arena {
+  cudaStream_t s;
+  std::vector<void*> ptrs;
+  explicit Arena(cudaStream_t st) : s(st) {}
+  ~Arena() {
+    for (void* p : ptrs) cudaFreeAsync(p, s);
+  }
+  template <typename T>
+  int alloc(T** p, uint64_t count) {
+    const size_t bytes = (size_t)std::max<uint64_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMallocAsync((void**)p, bytes, s);
+    if (e != cudaSuccess)
+      return set_error(e == cudaErrorMemoryAllocation ? SKC_ERR_OOM : SKC_ERR_CUDA,
+                       "device allocation of %zu bytes failed: %s", bytes,
+                       cudaGetErrorString(e));
+    ptrs.push_back((void*)*p);
+    return SKC_OK;
+  }
+  // Hands a buffer over to the caller (it is no longer freed here).
+  void release(void* p) {
+    auto it = std::find(ptrs.begin(), ptrs.end(), p);
+    if (it != ptrs.end()) ptrs.erase(it);
+  }
+};
+
+static inline uint64_t round_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
+
+static uint32_t bucket_count(uint64_t m) {
+  uint64_t k = m / 4;
+  if (k < 64) k = 64;
+  if (k > 65536) k = 65536;
+  return (uint32_t)k;
+}
+
+// Lattice-level rank of every mask: popcount ascending, then value.
+static int rank_table(skc_context* ctx, int d, const uint32_t** out) {
+  if (!ctx->d_rank_tables[d]) {
+    const uint32_t ns = 1u << d;
+    std::vector<uint32_t> order(ns), rank(ns);
+    for (uint32_t i = 0; i < ns; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [](uint32_t a, uint32_t b) {
+      return __builtin_popcount(a) < __builtin_popcount(b);
+    });
+    for (uint32_t i = 0; i < ns; ++i) rank[order[i]] = i;
+    uint32_t* p = nullptr;
+    SKC_CUDA(cudaMalloc(&p, ns * sizeof(uint32_t)));
+    SKC_CUDA(cudaMemcpy(p, rank.data(), ns * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    ctx->d_rank_tables[d] = p;
+  }
+  *out = ctx->d_rank_tables[d];
+  return SKC_OK;
+}
+
+// Device-side result of the full-space step.
+struct FullSpace {
+  uint4* cells = nullptr;    // by point id (depth of the call)
+  uint32_t* sky = nullptr;   // full-space skyline ids, ascending
+  uint32_t* ext = nullptr;   // full-space extended skyline ids, ascending
+  uint32_t* cand = nullptr;  // union, ascending
+  uint32_t* counts = nullptr;  // device [0]=|sky| [1]=|ext| [2]=|cand|
+  uint32_t h_counts[3] = {0, 0, 0};
+};
+
+static int run_full_space(skc_context* ctx, skc_dataset* ds, int depth,
+                          Arena& A, FullSpace& F, Tracer& T) {
+  cudaStream_t s = ctx->stream;
+  const uint64_t n = ds->n;
+  const int d = ds->d;
+  const uint32_t full = (1u << d) - 1;
+  uint32_t* d_n;
+  SKC_TRY(A.alloc(&d_n, 1));
+  SKC_TRY(launch_set_u32(s, d_n, (uint32_t)n));
+  float* pivots;
+  SKC_TRY(A.alloc(&pivots, (uint64_t)kMaxDims * kMaxPivots));
+  SKC_TRY(A.alloc(&F.cells, n));
+  SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, nullptr, d_n, n, depth, pivots, F.cells));
+  T.mark("full: pivots+cells");
+
+  const uint32_t K = bucket_count(n);
+  BucketScratch b;
+  SKC_TRY(A.alloc(&b.f, n));
+  SKC_TRY(A.alloc(&b.keys, n));
+  SKC_TRY(A.alloc(&b.counts, K + 1));
+  SKC_TRY(A.alloc(&b.cursor, K + 1));
+  SKC_TRY(A.alloc(&b.minmax, 2));
+  uint32_t *sorted, *hi;
+  SKC_TRY(A.alloc(&sorted, n));
+  SKC_TRY(A.alloc(&hi, n));
+  SKC_TRY(launch_bucket_order(s, ds->x, ds->n_pad, d, nullptr, d_n, n, full, K, b, sorted, hi));
+  T.mark("full: norm order");
+
+  uint8_t* status;
+  SKC_TRY(A.alloc(&status, n));
+  SkylineArgs a{sorted, hi, nullptr, F.cells, ds->x, ds->n_pad, d_n, n, full, status};
+  SKC_TRY(launch_skyline(s, d, a));
+  T.mark("full: skyline kernel");
+
+  const uint64_t nblk = (n + 1023) / 1024 + 1;
+  uint32_t *blk0, *blk1;
+  SKC_TRY(A.alloc(&blk0, nblk));
+  SKC_TRY(A.alloc(&blk1, nblk));
+  SKC_TRY(A.alloc(&F.counts, 3));
+  SKC_TRY(A.alloc(&F.sky, n));
+  SKC_TRY(A.alloc(&F.ext, n));
+  SKC_TRY(A.alloc(&F.cand, n));
+  SKC_TRY(launch_status_compact(s, status, nullptr, d_n, n, 0, blk0, blk1, F.sky, F.ext,
+                                F.counts + 0, F.counts + 1));
+  SKC_TRY(launch_status_compact(s, status, nullptr, d_n, n, 1, blk0, blk1, F.cand, nullptr,
+                                F.counts + 2, nullptr));
+  SKC_CUDA(cudaMemcpyAsync(F.h_counts, F.counts, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  SKC_CUDA(cudaStreamSynchronize(s));
+  T.mark("full: compaction");
+  return SKC_OK;
+}
+
+// Bitmaps of every candidate, then CSR compaction (BATCHED and PLAIN/MDMC).
+static int run_bitmaps(skc_context* ctx, skc_dataset* ds, const skc_options& o,
+                       int depth, int max_d, Arena& A, FullSpace& F,
+                       skc_result* R, Tracer& T) {
+  cudaStream_t s = ctx->stream;
+  const int d = ds->d;
+  const uint32_t nsub = 1u << d;
+  const uint32_t W = nsub >= 32 ? nsub / 32 : 1;
+  const uint64_t m = F.h_counts[2];
+  const uint64_t m_pad = round_up(m, 128);
+  uint32_t* m_ptr = F.counts + 2;
+  const bool want_ext = o.want_extended || o.algo == SKC_ALGO_SDSC;
+
+  float *xc, *xq;
+  SKC_TRY(A.alloc(&xc, (uint64_t)d * m_pad));
+  SKC_TRY(A.alloc(&xq, (uint64_t)d * m_pad));
+  SKC_TRY(launch_gather_soa(s, ds->x, ds->n_pad, d, F.cand, m_ptr, m, m_pad, xc));
+  float* pivots;
+  uint4 *cc, *qc, *bmin;
+  SKC_TRY(A.alloc(&pivots, (uint64_t)kMaxDims * kMaxPivots));
+  SKC_TRY(A.alloc(&cc, m));
+  SKC_TRY(A.alloc(&qc, m));
+  SKC_TRY(A.alloc(&bmin, (m + 31) / 32));
+  SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, F.cand, m_ptr, m, depth, pivots, cc));
+
+  const uint32_t* rank;
+  SKC_TRY(rank_table(ctx, d, &rank));
+  BucketScratch b;
+  SKC_TRY(A.alloc(&b.keys, m));
+  SKC_TRY(A.alloc(&b.counts, nsub + 1));
+  SKC_TRY(A.alloc(&b.cursor, nsub + 1));
+  uint32_t *qperm, *qids;
+  SKC_TRY(A.alloc(&qperm, m));
+  SKC_TRY(A.alloc(&qids, m));
+  SKC_TRY(launch_level_keys(s, cc, m_ptr, m, d, depth, rank, b.keys));
+  SKC_TRY(launch_counting_sort(s, b.keys, m_ptr, m, nsub, b, qperm, nullptr));
+  SKC_TRY(launch_gather_u32(s, F.cand, qperm, m_ptr, m, qids));
+  SKC_TRY(launch_gather_soa(s, ds->x, ds->n_pad, d, qids, m_ptr, m, m_pad, xq));
+  SKC_TRY(launch_gather_u4(s, cc, qperm, m_ptr, m, qc));
+  SKC_TRY(launch_block_min(s, qc, m_ptr, m, bmin));
+
+  T.mark("cand: cells+q order");
+  uint32_t *dom, *ext = nullptr, *work;
+  SKC_TRY(A.alloc(&dom, m * W));
+  if (want_ext) SKC_TRY(A.alloc(&ext, m * W));
+  SKC_TRY(A.alloc(&work, 1));
+
+  BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, m_ptr, work, 0xffffffffu, dom, ext, 0};
+  if (o.mode == SKC_MODE_BATCHED) {
+    SKC_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), s));
+    SKC_TRY(launch_bitmaps(s, d, ctx->num_sms, ba));
+  } else {
+    // One launch per batch of points with a host round trip after each
+    // (bitmaps of the batch copied to pinned host memory).
+    const uint32_t batch = d >= 16 ? 2300 : 5600;
+    uint32_t* h_stage = nullptr;
+    SKC_CUDA(cudaMallocHost(&h_stage, (size_t)batch * W * sizeof(uint32_t)));
+    int st = SKC_OK;
+    for (uint64_t p0 = 0; p0 < m && st == SKC_OK; p0 += batch) {
+      const uint32_t p1 = (uint32_t)std::min<uint64_t>(m, p0 + batch);
+      st = launch_set_u32(s, work, (uint32_t)p0);
+      if (st != SKC_OK) break;
+      ba.p_end = p1;
+      st = launch_bitmaps(s, d, ctx->num_sms, ba);
+      if (st != SKC_OK) break;
+      cudaError_t e = cudaMemcpyAsync(h_stage, dom + p0 * W, (size_t)(p1 - p0) * W * sizeof(uint32_t),
+                                      cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) st = set_error(SKC_ERR_CUDA, "batch copy failed: %s", cudaGetErrorString(e));
+    }
+    cudaFreeHost(h_stage);
+    SKC_TRY(st);
+  }
+  T.mark("bitmap kernel");
+
+  // Compaction of skylines (bit clear) and extended skylines (bit set).
+  const uint32_t tiles = compact_tiles(m);
+  const uint64_t C = 32ull * W;
+  for (int pass = 0; pass < (want_ext ? 2 : 1); ++pass) {
+    CompactArgs ca{};
+    ca.bits = pass == 0 ? dom : ext;
+    ca.words = W;
+    ca.m_ptr = m_ptr;
+    ca.m_max = m;
+    ca.count_set = pass;
+    ca.nsub = nsub;
+    ca.max_d = max_d;
+    ca.cand = F.cand;
+    SKC_TRY(A.alloc(&ca.counts, C * tiles));
+    SKC_TRY(A.alloc(&ca.offs, C * tiles + 1));
+    SKC_TRY(A.alloc(&ca.bsum, scan_bsum_entries(C * tiles)));
+    uint64_t* csr;
+    SKC_TRY(A.alloc(&csr, nsub + 1));
+    ca.csr_off = csr;
+    SKC_TRY(launch_bits_count(s, ca));
+    uint64_t total = 0;
+    SKC_CUDA(cudaMemcpyAsync(&total, csr + nsub, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    SKC_CUDA(cudaStreamSynchronize(s));
+    uint32_t* ids;
+    SKC_TRY(A.alloc(&ids, total));
+    ca.out = ids;
+    SKC_TRY(launch_bits_write(s, ca));
+    T.mark(pass == 0 ? "compaction: skylines" : "compaction: extended");
+    A.release(csr);
+    A.release(ids);
+    if (pass == 0) {
+      R->d_off = csr;
+      R->d_ids = ids;
+      R->total_ids = total;
+    } else {
+      R->d_eoff = csr;
+      R->d_eids = ids;
+      R->total_ext = total;
+    }
+  }
+  if (o.want_bitmaps) {
+    A.release(dom);
+    A.release(F.cand);
+    R->d_bits = dom;
+    R->d_cand = F.cand;
+    R->words = W;
+  }
+  return SKC_OK;
+}
+
+// The suite's per-cuboid schedule (PLAIN/SDSC).
+static int run_sdsc_plain(skc_context* ctx, skc_dataset* ds, int max_d,
+                          Arena& A, FullSpace& F, skc_result* R, Tracer& T) {
+  cudaStream_t s = ctx->stream;
+  const int d = ds->d;
+  const uint32_t nsub = 1u << d, full = nsub - 1;
+  std::vector<uint32_t*> sky(nsub, nullptr), ext(nsub, nullptr);
+  std::vector<uint64_t> nsky(nsub, 0), next(nsub, 0);
+  sky[full] = F.sky;
+  ext[full] = F.ext;
+  nsky[full] = F.h_counts[0];
+  next[full] = F.h_counts[1];
+
+  uint64_t mmax = nsky[full] + next[full];
+  const uint32_t K = bucket_count(mmax);
+  BucketScratch b;
+  SKC_TRY(A.alloc(&b.f, mmax));
+  SKC_TRY(A.alloc(&b.keys, mmax));
+  SKC_TRY(A.alloc(&b.counts, K + 1));
+  SKC_TRY(A.alloc(&b.cursor, K + 1));
+  SKC_TRY(A.alloc(&b.minmax, 2));
+  uint32_t *sorted, *hi, *cand, *d_m, *blk0, *blk1, *cnt;
+  uint8_t* status;
+  SKC_TRY(A.alloc(&sorted, mmax));
+  SKC_TRY(A.alloc(&hi, mmax));
+  SKC_TRY(A.alloc(&cand, mmax));
+  SKC_TRY(A.alloc(&status, mmax));
+  SKC_TRY(A.alloc(&d_m, 1));
+  const uint64_t nblk = (mmax + 1023) / 1024 + 1;
+  SKC_TRY(A.alloc(&blk0, nblk));
+  SKC_TRY(A.alloc(&blk1, nblk));
+  SKC_TRY(A.alloc(&cnt, 2));
+  uint32_t* h_cnt = nullptr;
+  SKC_CUDA(cudaMallocHost(&h_cnt, 2 * sizeof(uint32_t)));
+
+  int st = SKC_OK;
+  for (int lev = d - 1; lev >= 1 && st == SKC_OK; --lev) {
+    if (lev > max_d) continue;
+    for (uint32_t c = 1; c < full && st == SKC_OK; ++c) {
+      if (__builtin_popcount(c) != lev) continue;
+      // Parents in the order generate_lattice lists them (descending index).
+      uint32_t par[kMaxDims];
+      int np = 0;
+      for (int j = d - 1; j >= 0; --j)
+        if (!(c & (1u << j))) par[np++] = c | (1u << j);
+      uint32_t src = full;
+      if (nsky[par[0]] != 0) {
+        src = par[0];
+        uint64_t best = nsky[src] + next[src];
+        for (int i = 1; i < np; ++i) {
+          const uint64_t v = nsky[par[i]] + next[par[i]];
+          if (v < best) { best = v; src = par[i]; }
+        }
+      }
+      const uint64_t mc = nsky[src] + next[src];
+      if (mc == 0) continue;
+      auto fail = [&](int code) { st = code; };
+      // Candidates = parent skyline + extended skyline, merged ascending so
+      // every output list stays ascending (compaction keeps list order).
+      if ((st = launch_merge_disjoint(s, sky[src], (uint32_t)nsky[src], ext[src], (uint32_t)next[src], cand)) != SKC_OK) break;
+      cudaError_t e = cudaSuccess;
+      if ((st = launch_set_u32(s, d_m, (uint32_t)mc)) != SKC_OK) break;
+      if ((st = launch_bucket_order(s, ds->x, ds->n_pad, d, cand, d_m, mc, c, bucket_count(mc), b, sorted, hi)) != SKC_OK) break;
+      SkylineArgs a{sorted, hi, cand, F.cells, ds->x, ds->n_pad, d_m, mc, c, status};
+      if ((st = launch_skyline(s, d, a)) != SKC_OK) break;
+      uint32_t *osky, *oext;
+      if ((st = A.alloc(&osky, mc)) != SKC_OK) break;
+      if ((st = A.alloc(&oext, mc)) != SKC_OK) break;
+      if ((st = launch_status_compact(s, status, cand, d_m, mc, 0, blk0, blk1, osky, oext, cnt, cnt + 1)) != SKC_OK) break;
+      e = cudaMemcpyAsync(h_cnt, cnt, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) { fail(set_error(SKC_ERR_CUDA, "cuboid %u: %s", c, cudaGetErrorString(e))); break; }
+      sky[c] = osky;
+      ext[c] = oext;
+      nsky[c] = h_cnt[0];
+      next[c] = h_cnt[1];
+    }
+  }
+  cudaFreeHost(h_cnt);
+  SKC_TRY(st);
+  T.mark("per-cuboid skylines");
+
+  // Assemble cuboid-indexed CSRs of skylines and extended skylines.
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<uint64_t> off(nsub + 1, 0);
+    const auto& cntv = pass == 0 ? nsky : next;
+    const auto& srcv = pass == 0 ? sky : ext;
+    for (uint32_t c = 0; c < nsub; ++c) {
+      const bool want = c >= 1 && __builtin_popcount(c) <= max_d;
+      off[c + 1] = off[c] + (want ? cntv[c] : 0);
+    }
+    uint64_t* d_off;
+    uint32_t* ids;
+    const uint32_t** d_srcs;
+    SKC_TRY(A.alloc(&d_off, nsub + 1));
+    SKC_TRY(A.alloc(&ids, off[nsub]));
+    SKC_TRY(A.alloc(&d_srcs, nsub));
+    std::vector<const uint32_t*> srcs(nsub, nullptr);
+    for (uint32_t c = 0; c < nsub; ++c)
+      if (off[c + 1] > off[c]) srcs[c] = srcv[c];
+    SKC_CUDA(cudaMemcpyAsync(d_off, off.data(), (nsub + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    SKC_CUDA(cudaMemcpyAsync(d_srcs, srcs.data(), nsub * sizeof(void*), cudaMemcpyHostToDevice, s));
+    SKC_TRY(launch_csr_gather(s, d_srcs, d_off, nsub, ids));
+    SKC_CUDA(cudaStreamSynchronize(s));  // host vectors above must outlive the copies
+    A.release(d_off);
+    A.release(ids);
+    if (pass == 0) {
+      R->d_off = d_off;
+      R->d_ids = ids;
+      R->total_ids = off[nsub];
+    } else {
+      R->d_eoff = d_off;
+      R->d_eids = ids;
+      R->total_ext = off[nsub];
+    }
+  }
+  return SKC_OK;
+}
+
+static int auto_depth(uint64_t n, int d) {
+  (void)n;
+  (void)d;
+  return kMaxDepth;
+}
+
+}  // namespace skc
+
+using namespace skc;
+
+// Frees an object's device memory and detaches it from its context; the host
+// struct stays valid until the caller frees it.
+static void release_result_memory(skc_result* r) {
+  if (!r->ctx) return;
+  cudaStream_t s = r->ctx->stream;
+  for (void* p : {(void*)r->d_off, (void*)r->d_ids, (void*)r->d_eoff, (void*)r->d_eids,
+                  (void*)r->d_bits, (void*)r->d_cand})
+    if (p) cudaFreeAsync(p, s);
+  r->d_off = nullptr;
+  r->d_ids = nullptr;
+  r->d_eoff = nullptr;
+  r->d_eids = nullptr;
+  r->d_bits = nullptr;
+  r->d_cand = nullptr;
+  r->ctx->results.erase(r);
+  r->ctx = nullptr;
+}
+
+static void release_dataset_memory(skc_dataset* ds) {
+  if (!ds->ctx) return;
+  if (ds->x) cudaFreeAsync(ds->x, ds->ctx->stream);
+  ds->x = nullptr;
+  ds->ctx->datasets.erase(ds);
+  ds->ctx = nullptr;
+}
+
+// ==========================================================================
+// C ABI
+extern "C" {
+
+const char* skc_last_error(void) { return g_err.c_str(); }
+
+uint64_t skc_kernel_launches(void) { return g_launches.load(); }
+
+int skc_last_phase(skc_context* ctx, int index, const char** name, float* ms) {
+  clear_error();
+  if (!ctx || !name || !ms) return set_error(SKC_ERR_INVALID, "NULL argument");
+  if (index < 0 || index >= (int)ctx->phases.size())
+    return set_error(SKC_ERR_INVALID, "phase %d out of range (%d phases)", index, (int)ctx->phases.size());
+  *name = ctx->phases[index].first.c_str();
+  *ms = ctx->phases[index].second;
+  return SKC_OK;
+}
+
+void skc_options_init(skc_options* o) {
+  if (!o) return;
+  o->algo = SKC_ALGO_MDMC;
+  o->mode = SKC_MODE_BATCHED;
+  o->max_d = 0;
+  o->depth = 0;
+  o->want_extended = 0;
+  o->want_bitmaps = 0;
+}
+
+int skc_context_create(int device, skc_context** out) {
+  clear_error();
+  if (!out) return set_error(SKC_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess) return set_error(SKC_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+  if (device < 0 || device >= count)
+    return set_error(SKC_ERR_INVALID, "device %d out of range (%d devices)", device, count);
+  SKC_CUDA(cudaSetDevice(device));
+  SKC_CUDA(cudaFree(0));
+  auto* ctx = new skc_context;
+  ctx->device = device;
+  if (cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&ctx->ev_start) != cudaSuccess || cudaEventCreate(&ctx->ev_stop) != cudaSuccess ||
+      cudaDeviceGetDefaultMemPool(&ctx->pool, device) != cudaSuccess) {
+    delete ctx;
+    return set_error(SKC_ERR_CUDA, "context setup failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  uint64_t thr = UINT64_MAX;
+  cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  upload_submask_table();
+  *out = ctx;
+  return SKC_OK;
+}
+
+int skc_context_destroy(skc_context* ctx) {
+  clear_error();
+  if (!ctx) return SKC_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (skc_result* r : std::vector<skc_result*>(ctx->results.begin(), ctx->results.end()))
+    release_result_memory(r);
+  for (skc_dataset* ds : std::vector<skc_dataset*>(ctx->datasets.begin(), ctx->datasets.end()))
+    release_dataset_memory(ds);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto* p : ctx->d_rank_tables)
+    if (p) cudaFree(p);
+  cudaEventDestroy(ctx->ev_start);
+  cudaEventDestroy(ctx->ev_stop);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return SKC_OK;
+}
+
+static int upload_common(skc_context* ctx, const float* rows, uint64_t n, int d,
+                         bool from_host, skc_dataset** out) {
+  clear_error();
+  if (!ctx || !rows || !out) return set_error(SKC_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (d < SKC_MIN_DIMS || d > SKC_MAX_DIMS)
+    return set_error(SKC_ERR_INVALID, "d=%d outside [%d,%d]", d, SKC_MIN_DIMS, SKC_MAX_DIMS);
+  if (n == 0) return set_error(SKC_ERR_INVALID, "empty dataset (n=0)");
+  if (n > 0xffffff00ull) return set_error(SKC_ERR_UNSUPPORTED, "n=%llu exceeds 32-bit point ids", (unsigned long long)n);
+  SKC_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  auto* ds = new skc_dataset;
+  ds->ctx = ctx;
+  ds->n = n;
+  ds->d = d;
+  ds->n_pad = round_up(n, 128);
+  Arena A(s);
+  int st = SKC_OK;
+  const float* d_rows = rows;
+  uint32_t* bad = nullptr;
+  uint32_t h_bad = 0;
+  do {
+    cudaError_t e = cudaMallocAsync((void**)&ds->x, (size_t)d * ds->n_pad * sizeof(float), s);
+    if (e != cudaSuccess) { st = set_error(SKC_ERR_OOM, "dataset allocation failed: %s", cudaGetErrorString(e)); break; }
+    if (from_host) {
+      float* tmp;
+      if ((st = A.alloc(&tmp, n * d)) != SKC_OK) break;
+      e = cudaMemcpyAsync(tmp, rows, n * d * sizeof(float), cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) { st = set_error(SKC_ERR_CUDA, "upload copy failed: %s", cudaGetErrorString(e)); break; }
+      d_rows = tmp;
+    }
+    if ((st = A.alloc(&bad, 1)) != SKC_OK) break;
+    if (cudaMemsetAsync(bad, 0, sizeof(uint32_t), s) != cudaSuccess) { st = set_error(SKC_ERR_CUDA, "memset"); break; }
+    if ((st = launch_rows_to_soa(s, d_rows, n, d, ds->n_pad, ds->x, bad)) != SKC_OK) break;
+    e = cudaMemcpyAsync(&h_bad, bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { st = set_error(SKC_ERR_CUDA, "upload failed: %s", cudaGetErrorString(e)); break; }
+    if (h_bad) st = set_error(SKC_ERR_INVALID, "%u non-finite attribute values (NaN/inf) rejected", h_bad);
+  } while (0);
+  if (st != SKC_OK) {
+    if (ds->x) cudaFreeAsync(ds->x, s);
+    delete ds;
+    return st;
+  }
+  ctx->datasets.insert(ds);
+  *out = ds;
+  return SKC_OK;
+}
+
+int skc_dataset_upload(skc_context* ctx, const float* rows, uint64_t n, int d, skc_dataset** out) {
+  return upload_common(ctx, rows, n, d, true, out);
+}
+
+int skc_dataset_upload_device(skc_context* ctx, const float* d_rows, uint64_t n, int d,
+                              skc_dataset** out) {
+  return upload_common(ctx, d_rows, n, d, false, out);
+}
+
+int skc_dataset_free(skc_dataset* ds) {
+  clear_error();
+  if (!ds) return SKC_OK;
+  if (ds->ctx) {
+    skc_context* ctx = ds->ctx;
+    cudaSetDevice(ctx->device);
+    release_dataset_memory(ds);
+    cudaStreamSynchronize(ctx->stream);
+  }
+  delete ds;
+  return SKC_OK;
+}
+
+int skc_skycube(skc_context* ctx, skc_dataset* ds, const skc_options* opt, skc_result** out) {
+  clear_error();
+  if (!ctx || !ds || !out) return set_error(SKC_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (ds->ctx != ctx) return set_error(SKC_ERR_INVALID, "dataset belongs to another (or a destroyed) context");
+  skc_options o;
+  skc_options_init(&o);
+  if (opt) o = *opt;
+  if (o.algo != SKC_ALGO_MDMC && o.algo != SKC_ALGO_SDSC)
+    return set_error(SKC_ERR_INVALID, "unknown algorithm %d", o.algo);
+  if (o.mode != SKC_MODE_PLAIN && o.mode != SKC_MODE_BATCHED)
+    return set_error(SKC_ERR_INVALID, "unknown mode %d", o.mode);
+  if (o.depth < 0 || o.depth > kMaxDepth)
+    return set_error(SKC_ERR_INVALID, "depth %d outside [1,%d] (0 = auto)", o.depth, kMaxDepth);
+  const int d = ds->d;
+  const int max_d = (o.max_d <= 0 || o.max_d > d) ? d : o.max_d;
+  const int depth = o.depth ? o.depth : auto_depth(ds->n, d);
+  SKC_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+
+  auto* R = new skc_result;
+  R->ctx = ctx;
+  R->d = d;
+  R->max_d = max_d;
+  R->algo = o.algo;
+  int st = SKC_OK;
+  {
+    Arena A(s);
+    FullSpace F;
+    cudaEventRecord(ctx->ev_start, s);
+    Tracer T(ctx);
+    st = run_full_space(ctx, ds, depth, A, F, T);
+    if (st == SKC_OK) {
+      R->n_cand = F.h_counts[2];
+      if (o.algo == SKC_ALGO_SDSC && o.mode == SKC_MODE_PLAIN) {
+        A.release(F.sky);
+        A.release(F.ext);
+        st = run_sdsc_plain(ctx, ds, max_d, A, F, R, T);
+        cudaFreeAsync(F.sky, s);
+        cudaFreeAsync(F.ext, s);
+      } else {
+        st = run_bitmaps(ctx, ds, o, depth, max_d, A, F, R, T);
+      }
+    }
+    cudaEventRecord(ctx->ev_stop, s);
+  }
+  if (st == SKC_OK) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = set_error(SKC_ERR_CUDA, "skycube failed: %s", cudaGetErrorString(e));
+  }
+  if (st == SKC_OK) cudaEventElapsedTime(&ctx->last_ms, ctx->ev_start, ctx->ev_stop);
+  if (st != SKC_OK) {
+    std::string msg = g_err;
+    skc_result_free(R);
+    g_err = msg;
+    return st;
+  }
+  ctx->results.insert(R);
+  *out = R;
+  return SKC_OK;
+}
+
+int skc_result_info(skc_result* r, int* d, uint64_t* n_cand, uint64_t* total) {
+  clear_error();
+  if (!r) return set_error(SKC_ERR_INVALID, "NULL result");
+  if (d) *d = r->d;
+  if (n_cand) *n_cand = r->n_cand;
+  if (total) *total = r->total_ids;
+  return SKC_OK;
+}
+
+static int download_csr(skc_result* r, bool ext) {
+  bool& done = ext ? r->ext_downloaded : r->downloaded;
+  if (done) return SKC_OK;
+  if (!r->ctx) return set_error(SKC_ERR_INVALID, "result's context was destroyed");
+  const uint64_t* d_off = ext ? r->d_eoff : r->d_off;
+  const uint32_t* d_ids = ext ? r->d_eids : r->d_ids;
+  if (!d_off) return set_error(SKC_ERR_INVALID, ext ? "extended skylines were not requested" : "no skylines");
+  auto& off = ext ? r->h_eoff : r->h_off;
+  auto& ids = ext ? r->h_eids : r->h_ids;
+  const uint32_t nsub = 1u << r->d;
+  cudaStream_t s = r->ctx->stream;
+  SKC_CUDA(cudaSetDevice(r->ctx->device));
+  off.resize(nsub + 1);
+  SKC_CUDA(cudaMemcpyAsync(off.data(), d_off, (nsub + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  SKC_CUDA(cudaStreamSynchronize(s));
+  ids.resize(off[nsub]);
+  if (off[nsub])
+    SKC_CUDA(cudaMemcpyAsync(ids.data(), d_ids, off[nsub] * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  SKC_CUDA(cudaStreamSynchronize(s));
+  done = true;
+  return SKC_OK;
+}
+
+int skc_result_download(skc_result* r) {
+  clear_error();
+  if (!r) return set_error(SKC_ERR_INVALID, "NULL result");
+  return download_csr(r, false);
+}
+
+static int cuboid_view(skc_result* r, uint32_t c, bool ext, const uint32_t** ids, uint64_t* count) {
+  clear_error();
+  if (!r || !ids || !count) return set_error(SKC_ERR_INVALID, "NULL argument");
+  if (c == 0 || c >= (1u << r->d)) return set_error(SKC_ERR_INVALID, "cuboid %u outside [1, 2^%d)", c, r->d);
+  SKC_TRY(download_csr(r, ext));
+  const auto& off = ext ? r->h_eoff : r->h_off;
+  const auto& v = ext ? r->h_eids : r->h_ids;
+  *count = off[c + 1] - off[c];
+  *ids = v.data() + off[c];
+  return SKC_OK;
+}
+
+int skc_result_cuboid(skc_result* r, uint32_t c, const uint32_t** ids, uint64_t* count) {
+  return cuboid_view(r, c, false, ids, count);
+}
+
+int skc_result_extended(skc_result* r, uint32_t c, const uint32_t** ids, uint64_t* count) {
+  return cuboid_view(r, c, true, ids, count);
+}
+
+int skc_result_device_csr(skc_result* r, const uint64_t** d_off, const uint32_t** d_ids) {
+  clear_error();
+  if (!r || !d_off || !d_ids) return set_error(SKC_ERR_INVALID, "NULL argument");
+  *d_off = r->d_off;
+  *d_ids = r->d_ids;
+  return SKC_OK;
+}
+
+int skc_result_bitmaps(skc_result* r, const uint32_t** bits, const uint32_t** pids,
+                       uint64_t* n_points, uint32_t* words) {
+  clear_error();
+  if (!r || !bits || !pids || !n_points || !words) return set_error(SKC_ERR_INVALID, "NULL argument");
+  if (!r->bits_downloaded && !r->ctx) return set_error(SKC_ERR_INVALID, "result's context was destroyed");
+  if (!r->bits_downloaded && !r->d_bits) return set_error(SKC_ERR_INVALID, "bitmaps were not requested (want_bitmaps)");
+  if (!r->bits_downloaded) {
+    SKC_CUDA(cudaSetDevice(r->ctx->device));
+    cudaStream_t s = r->ctx->stream;
+    r->h_bits.resize(r->n_cand * r->words);
+    r->h_cand.resize(r->n_cand);
+    if (r->n_cand) {
+      SKC_CUDA(cudaMemcpyAsync(r->h_bits.data(), r->d_bits, r->h_bits.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      SKC_CUDA(cudaMemcpyAsync(r->h_cand.data(), r->d_cand, r->n_cand * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    }
+    SKC_CUDA(cudaStreamSynchronize(s));
+    r->bits_downloaded = true;
+  }
+  *bits = r->h_bits.data();
+  *pids = r->h_cand.data();
+  *n_points = r->n_cand;
+  *words = r->words;
+  return SKC_OK;
+}
+
+int skc_result_free(skc_result* r) {
+  if (!r) return SKC_OK;
+  if (r->ctx) {
+    skc_context* ctx = r->ctx;
+    cudaSetDevice(ctx->device);
+    release_result_memory(r);
+    cudaStreamSynchronize(ctx->stream);
+  }
+  delete r;
+  return SKC_OK;
+}
+
+int skc_last_device_ms(skc_context* ctx, float* ms) {
+  clear_error();
+  if (!ctx || !ms) return set_error(SKC_ERR_INVALID, "NULL argument");
+  *ms = ctx->last_ms;
+  return SKC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+// Launch helpers of the skycube engine's kernels (internal).
+#pragma once
+
+#include "common.cuh"
+
+namespace skc {
+
+constexpr int kMaxDims = 16;
+constexpr int kMaxPivots = 127;  // 2^kMaxDepth - 1
+
+// Scratch of the counting sort by bucket (all device pointers).
+struct BucketScratch {
+  float* f = nullptr;        // [m_max] scores
+  uint32_t* keys = nullptr;  // [m_max]
+  uint32_t* counts = nullptr;  // [K + 1]
+  uint32_t* cursor = nullptr;  // [K + 1]
+  uint32_t* minmax = nullptr;  // [2]
+};
+
+// prep.cu
+int launch_rows_to_soa(cudaStream_t s, const float* rows, uint64_t n, int d,
+                       uint64_t n_pad, float* x, uint32_t* bad);
+int launch_iota(cudaStream_t s, uint32_t* out, uint64_t n);
+int launch_bucket_order(cudaStream_t s, const float* x, uint64_t n_pad, int d,
+                        const uint32_t* ids, const uint32_t* m_ptr,
+                        uint64_t m_max, uint32_t S, uint32_t K,
+                        const BucketScratch& b, uint32_t* sorted, uint32_t* hi);
+int launch_counting_sort(cudaStream_t s, const uint32_t* keys,
+                         const uint32_t* m_ptr, uint64_t m_max, uint32_t K,
+                         const BucketScratch& b, uint32_t* sorted, uint32_t* hi);
+int launch_pivots_cells(cudaStream_t s, const float* x, uint64_t n_pad, int d,
+                        const uint32_t* ids, const uint32_t* m_ptr,
+                        uint64_t m_max, int depth, float* pivots, uint4* cells);
+int launch_status_compact(cudaStream_t s, const uint8_t* st, const uint32_t* ids,
+                          const uint32_t* m_ptr, uint64_t m_max, int merge01,
+                          uint32_t* blk0, uint32_t* blk1, uint32_t* out0,
+                          uint32_t* out1, uint32_t* n0, uint32_t* n1);
+int launch_scan_u32_to_u64(cudaStream_t s, const uint32_t* in, uint64_t len,
+                           uint64_t* bsum, uint64_t* out);
+uint64_t scan_bsum_entries(uint64_t len);
+int launch_gather_soa(cudaStream_t s, const float* x, uint64_t n_pad, int d,
+                      const uint32_t* ids, const uint32_t* m_ptr, uint64_t m_max,
+                      uint64_t out_pad, float* out);
+int launch_gather_u4(cudaStream_t s, const uint4* in, const uint32_t* perm,
+                     const uint32_t* m_ptr, uint64_t m_max, uint4* out);
+int launch_level_keys(cudaStream_t s, const uint4* cells, const uint32_t* m_ptr,
+                      uint64_t m_max, int d, int depth, const uint32_t* rank,
+                      uint32_t* keys);
+int launch_block_min(cudaStream_t s, const uint4* cells, const uint32_t* m_ptr,
+                     uint64_t m_max, uint4* bmin);
+int launch_csr_gather(cudaStream_t s, const uint32_t* const* srcs,
+                      const uint64_t* dst_off, uint32_t ncub, uint32_t* dst);
+int launch_set_u32(cudaStream_t s, uint32_t* p, uint32_t v);
+int launch_merge_disjoint(cudaStream_t s, const uint32_t* a, uint32_t na,
+                          const uint32_t* b, uint32_t nb, uint32_t* out);
+int launch_gather_u32(cudaStream_t s, const uint32_t* in, const uint32_t* perm,
+                      const uint32_t* m_ptr, uint64_t m_max, uint32_t* out);
+int launch_csr_assemble(cudaStream_t s, const uint32_t* src,
+                        const uint64_t* src_off, const uint64_t* dst_off,
+                        uint32_t ncub, uint32_t* dst);
+
+// skyline.cu: status of every list entry on subspace S (0 skyline,
+// 1 extended skyline, 2 strictly dominated).
+struct SkylineArgs {
+  const uint32_t* sorted;  // sorted index -> list position (bucket order)
+  const uint32_t* hi;      // sorted index -> end of its bucket
+  const uint32_t* ids;     // list position -> point id (nullptr: identity)
+  const uint4* cells;      // point id -> grid cells
+  const float* x;          // attribute-major points
+  uint64_t n_pad;
+  const uint32_t* m_ptr;   // list length (device)
+  uint64_t m_max;          // upper bound of the list length (host)
+  uint32_t S;              // subspace mask
+  uint8_t* status;         // list position -> status
+};
+int launch_skyline(cudaStream_t s, int d, const SkylineArgs& a);
+
+// mdmc.cu: per-point dominated-subspace bitmaps over the candidate set.
+struct BitmapArgs {
+  const uint4* pcells;   // candidate order
+  const float* px;       // candidate order, attribute-major, pitch p_pad
+  uint64_t p_pad;
+  const uint4* qcells;   // q order (level-sorted)
+  const float* qx;       // q order, attribute-major, pitch p_pad
+  const uint4* bmin;     // per block of 32 q's
+  const uint32_t* m_ptr;
+  uint32_t* work;        // work counter, must hold p_begin
+  uint32_t p_end;        // stop at min(m, p_end)
+  uint32_t* out_dom;     // [m][words] dominated bitmaps
+  uint32_t* out_ext;     // [m][words] extended-skyline bitmaps, or nullptr
+  int grid_blocks;       // persistent grid (0: from occupancy)
+};
+int launch_bitmaps(cudaStream_t s, int d, int num_sms, const BitmapArgs& a);
+
+struct CompactArgs {
+  const uint32_t* bits;  // [m][words]
+  uint32_t words;
+  const uint32_t* m_ptr;
+  uint64_t m_max;
+  int count_set;         // 0: rows with the bit CLEAR (skyline); 1: SET
+  uint32_t nsub;         // 2^d
+  int max_d;
+  const uint32_t* cand;  // row -> point id
+  uint32_t* counts;      // [32*words * tiles]
+  uint64_t* offs;        // [32*words * tiles + 1]
+  uint64_t* bsum;        // scan scratch
+  uint64_t* csr_off;     // [nsub + 1] output offsets per cuboid
+  uint32_t* out;         // ids (sized by the caller after the count pass)
+};
+uint32_t compact_tiles(uint64_t m_max);
+int launch_bits_count(cudaStream_t s, const CompactArgs& a);
+int launch_bits_write(cudaStream_t s, const CompactArgs& a);
+
+void upload_submask_table();
+
+}  // namespace skc

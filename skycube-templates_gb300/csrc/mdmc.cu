@@ -1,0 +1,401 @@
+// Per-point dominated-subspace bitmaps over the candidate set (the MDMC
+// computation of the suite: produce_bitmap_iterative_multi_partition_
+// templated_async, src/utilities/kernels.cuh:415-908, driven by
+// tombstoning_hearting_gpu, src/mdmc/MDMC.cu:752-857), and their compaction
+// into per-cuboid id lists (HashCube decode, src/utilities/utilities.h:
+// 253-267, done on the device).
+//
+// For a point p and another point q let LE = {k : q[k] <= p[k]} and
+// LT = {k : q[k] < p[k]}. q dominates p exactly on the subspaces S with
+// S subset of LE and S meeting LT, and strictly dominates p on the non-empty
+// subsets of LT. Two bitmaps over all 2^d subspaces are kept per p:
+//   STRICT = union over q of down(LT)      (down-closed)
+//   TIE    = union over q with LE != LT of {S subset of LE, S not subset of
+//            EQ}, EQ = LE \ LT            (only exact float ties feed it)
+// Then p is dominated on S iff S in STRICT or TIE, and p is in the extended
+// skyline of S iff S in TIE and not in STRICT.
+//
+// Pruning. Grid cells (common.cuh) give, without touching floats, the set U
+// of attributes where q may be <= p (LE subset of U). If U is in STRICT, the
+// down-closure of U is already strict and q adds nothing. The same test on
+// the byte-wise minimum cells of a block of 32 consecutive q's skips the
+// whole block. q's are ordered by the lattice level of their median mask so
+// the strongest points come first and STRICT fills early.
+//
+// Mapping. One warp owns one p at a time (a persistent grid pulls p's from a
+// device counter) and its 32 lanes test 32 q's per step. For d <= 10 the
+// 2^d-bit STRICT and TIE bitmaps live in registers, one 32-bit word per lane
+// (word w in lane w); a membership test is one shuffle. For d >= 11 they
+// live in shared memory, one pair per warp. A new (LE, LT) pair is applied
+// word-parallel: word w of down(L) is submask(L & 31) if w is a subset of
+// L >> 5, else empty.
+#include "kernels.cuh"
+
+namespace skc {
+
+// c_submask[x] = bit b set iff b is a subset of x (5-bit masks).
+__constant__ uint32_t c_submask[32];
+
+void upload_submask_table() {
+  uint32_t t[32];
+  for (uint32_t x = 0; x < 32; ++x) {
+    uint32_t m = 0;
+    for (uint32_t b = 0; b < 32; ++b)
+      if ((b & ~x) == 0) m |= 1u << b;
+    t[x] = m;
+  }
+  cudaMemcpyToSymbol(c_submask, t, sizeof(t));
+}
+
+constexpr uint32_t kFull = 0xffffffffu;
+
+template <int D>
+struct BitState {
+  static constexpr uint32_t NSUB = 1u << D;
+  static constexpr uint32_t W = NSUB >= 32 ? NSUB / 32 : 1;
+  static constexpr bool REG = (W <= 32);
+};
+
+template <int D>
+__global__ void __launch_bounds__(256) k_bitmaps(
+    const uint4* __restrict__ pcells, const float* __restrict__ px,
+    uint64_t p_pad, const uint4* __restrict__ qcells,
+    const float* __restrict__ qx, const uint4* __restrict__ bmin,
+    const uint32_t* __restrict__ m_ptr, uint32_t* __restrict__ work,
+    uint32_t p_end_cap, uint32_t* __restrict__ out_dom,
+    uint32_t* __restrict__ out_ext) {
+  using BS = BitState<D>;
+  constexpr int NW = (D + 3) / 4;
+  constexpr uint32_t NSUB = BS::NSUB;
+  constexpr uint32_t W = BS::W;
+  constexpr bool REG = BS::REG;
+  extern __shared__ uint32_t smem[];
+
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  uint32_t* sat_s = REG ? nullptr : smem + (size_t)wib * 2 * W;
+  uint32_t* tie_s = REG ? nullptr : sat_s + W;
+  const uint32_t m = *m_ptr;
+  const uint32_t pend = min(m, p_end_cap);
+  const uint32_t nblk = (m + 31) / 32;
+  const uint32_t wi = REG ? (uint32_t)lane % W : 0;
+
+  for (;;) {
+    uint32_t p = 0;
+    if (lane == 0) p = atomicAdd(work, 1u);
+    p = __shfl_sync(kFull, p, 0);
+    if (p >= pend) break;
+
+    const uint4 pc4 = pcells[p];
+    uint32_t pc[NW], pH[NW];
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      pc[w] = word_of(pc4, w);
+      pH[w] = pc[w] | kGuard;
+    }
+    float pv[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) pv[k] = px[(uint64_t)k * p_pad + p];
+
+    // STRICT starts with the empty subspace so that q's worse on every
+    // attribute (U == 0) test as "nothing new".
+    uint32_t sat = 0, tie = 0;
+    if (REG) {
+      sat = (wi == 0) ? 1u : 0u;
+    } else {
+      for (uint32_t w = lane; w < W; w += 32) {
+        sat_s[w] = (w == 0) ? 1u : 0u;
+        tie_s[w] = 0;
+      }
+      __syncwarp();
+    }
+    auto in_strict = [&](uint32_t S) -> bool {
+      uint32_t word;
+      if (REG) word = __shfl_sync(kFull, sat, S >> 5);
+      else word = sat_s[S >> 5];
+      return (word >> (S & 31)) & 1u;
+    };
+
+    for (uint32_t b = 0; b < nblk; ++b) {
+      const uint4 bm = bmin[b];
+      uint32_t Ub = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w)
+        Ub |= pack_guards(ge_bytes(pH[w], word_of(bm, w))) << (4 * w);
+      Ub &= NSUB - 1;
+      if (in_strict(Ub)) continue;  // uniform: the whole block adds nothing
+
+      const uint32_t qi = b * 32 + lane;
+      const bool valid = qi < m;
+      uint4 q4 = make_uint4(0, 0, 0, 0);
+      if (valid) q4 = qcells[qi];
+      uint32_t U = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w)
+        U |= pack_guards(ge_bytes(pH[w], word_of(q4, w))) << (4 * w);
+      U = valid ? (U & (NSUB - 1)) : 0u;
+      const bool hit = in_strict(U);
+      if (__all_sync(kFull, hit)) continue;
+
+      uint32_t le = 0, lt = 0;
+      if (!hit) {
+        uint32_t G = 0;  // cell(q) >= cell(p)
+#pragma unroll
+        for (int w = 0; w < NW; ++w)
+          G |= pack_guards(ge_bytes(word_of(q4, w) | kGuard, pc[w])) << (4 * w);
+        G &= NSUB - 1;
+        const uint32_t Y = U & ~G;  // certainly q < p
+        const uint32_t Z = U & G;   // equal cells: compare the floats
+        le = Y;
+        lt = Y;
+        if (Z) {
+#pragma unroll
+          for (int k = 0; k < D; ++k) {
+            if (Z & (1u << k)) {
+              const float a = qx[(uint64_t)k * p_pad + qi];
+              if (a <= pv[k]) le |= 1u << k;
+              if (a < pv[k]) lt |= 1u << k;
+            }
+          }
+        }
+      }
+      const bool t_lt = in_strict(lt);
+      const bool t_le = in_strict(le);
+      const bool novel = !hit && (!t_lt || (le != lt && !t_le));
+      uint32_t todo = __ballot_sync(kFull, novel);
+      while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const uint32_t L = __shfl_sync(kFull, lt, src);
+        const uint32_t E = __shfl_sync(kFull, le, src);
+        const uint32_t Q = E & ~L;  // attributes with exact ties
+        if (REG) {
+          if ((wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
+          if (E != L && (wi & ~(E >> 5)) == 0) {
+            uint32_t mk = c_submask[E & 31];
+            if ((wi & ~(Q >> 5)) == 0) mk &= ~c_submask[Q & 31];
+            tie |= mk;
+          }
+        } else {
+          const uint32_t sl = c_submask[L & 31];
+          const uint32_t se = c_submask[E & 31];
+          const uint32_t sq = c_submask[Q & 31];
+          for (uint32_t w = lane; w < W; w += 32) {
+            if ((w & ~(L >> 5)) == 0) sat_s[w] |= sl;
+            if (E != L && (w & ~(E >> 5)) == 0)
+              tie_s[w] |= ((w & ~(Q >> 5)) == 0) ? (se & ~sq) : se;
+          }
+          __syncwarp();
+        }
+      }
+    }
+
+    // Output: dominated = STRICT | TIE, extended = TIE \ STRICT. Bit 0 (the
+    // empty subspace) is cleared.
+    if (REG) {
+      if ((uint32_t)lane < W) {
+        uint32_t dom = sat | tie, ext = tie & ~sat;
+        if (lane == 0) {
+          dom &= ~1u;
+          ext &= ~1u;
+        }
+        out_dom[(uint64_t)p * W + lane] = dom;
+        if (out_ext) out_ext[(uint64_t)p * W + lane] = ext;
+      }
+    } else {
+      for (uint32_t w = lane; w < W; w += 32) {
+        uint32_t s_ = sat_s[w], t_ = tie_s[w];
+        uint32_t dom = s_ | t_, ext = t_ & ~s_;
+        if (w == 0) {
+          dom &= ~1u;
+          ext &= ~1u;
+        }
+        out_dom[(uint64_t)p * W + w] = dom;
+        if (out_ext) out_ext[(uint64_t)p * W + w] = ext;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+template <int D>
+static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
+  using BS = BitState<D>;
+  constexpr int threads = 256;
+  const size_t smem = BS::REG ? 0 : (size_t)(threads / 32) * 2 * BS::W * sizeof(uint32_t);
+  if (smem > 48 * 1024)
+    SKC_CUDA(cudaFuncSetAttribute(k_bitmaps<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int grid = a.grid_blocks;
+  if (grid <= 0) {
+    int per_sm = 0;
+    SKC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmaps<D>, threads, smem));
+    if (per_sm < 1) per_sm = 1;
+    grid = per_sm * num_sms;
+  }
+  k_bitmaps<D><<<grid, threads, smem, s>>>(a.pcells, a.px, a.p_pad, a.qcells, a.qx,
+                                           a.bmin, a.m_ptr, a.work, a.p_end,
+                                           a.out_dom, a.out_ext);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
+int launch_bitmaps(cudaStream_t s, int d, int num_sms, const BitmapArgs& a) {
+  switch (d) {
+    case 2: return launch_bitmaps_d<2>(s, num_sms, a);
+    case 3: return launch_bitmaps_d<3>(s, num_sms, a);
+    case 4: return launch_bitmaps_d<4>(s, num_sms, a);
+    case 5: return launch_bitmaps_d<5>(s, num_sms, a);
+    case 6: return launch_bitmaps_d<6>(s, num_sms, a);
+    case 7: return launch_bitmaps_d<7>(s, num_sms, a);
+    case 8: return launch_bitmaps_d<8>(s, num_sms, a);
+    case 9: return launch_bitmaps_d<9>(s, num_sms, a);
+    case 10: return launch_bitmaps_d<10>(s, num_sms, a);
+    case 11: return launch_bitmaps_d<11>(s, num_sms, a);
+    case 12: return launch_bitmaps_d<12>(s, num_sms, a);
+    case 13: return launch_bitmaps_d<13>(s, num_sms, a);
+    case 14: return launch_bitmaps_d<14>(s, num_sms, a);
+    case 15: return launch_bitmaps_d<15>(s, num_sms, a);
+    case 16: return launch_bitmaps_d<16>(s, num_sms, a);
+    default: return set_error(SKC_ERR_INVALID, "unsupported d=%d", d);
+  }
+}
+
+// --------------------------------------------------------------------------
+// Compaction of bitmaps into per-cuboid id lists. Rows are cut in tiles of
+// kTileRows; a CTA handles one (tile, word) pair with 8 warps, warp k owning
+// rows [k*256, k*256+256) of the tile, so ids come out ascending per cuboid.
+constexpr uint32_t kTileRows = 2048;
+
+uint32_t compact_tiles(uint64_t m_max) {
+  uint64_t t = (m_max + kTileRows - 1) / kTileRows;
+  return (uint32_t)(t ? t : 1);
+}
+
+__device__ __forceinline__ bool cuboid_wanted(uint32_t c, uint32_t nsub, int max_d) {
+  return c >= 1 && c < nsub && __popc(c) <= max_d;
+}
+
+// Bits of row r's word w that count (1 = counted).
+__device__ __forceinline__ uint32_t counted_bits(const uint32_t* bits, uint32_t W,
+                                                 uint32_t r, uint32_t m, uint32_t w,
+                                                 int count_set) {
+  if (r >= m) return 0u;
+  const uint32_t v = bits[(uint64_t)r * W + w];
+  return count_set ? v : ~v;
+}
+
+__global__ void __launch_bounds__(256) k_bits_count(
+    const uint32_t* __restrict__ bits, uint32_t W,
+    const uint32_t* __restrict__ m_ptr, uint32_t T, int count_set,
+    uint32_t nsub, int max_d, uint32_t* __restrict__ counts) {
+  __shared__ uint32_t wc[8][32];
+  const uint32_t t = blockIdx.x, w = blockIdx.y;
+  const int lane = threadIdx.x & 31, k = threadIdx.x >> 5;
+  const uint32_t m = *m_ptr;
+  uint32_t cnt = 0;
+  const uint32_t row0 = t * kTileRows + k * 256;
+  if (t * kTileRows < m) {
+    for (int s = 0; s < 8; ++s) {
+      const uint32_t v = counted_bits(bits, W, row0 + s * 32 + lane, m, w, count_set);
+#pragma unroll
+      for (int b = 0; b < 32; ++b) {
+        const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
+        if (lane == b) cnt += __popc(bal);
+      }
+    }
+  }
+  wc[k][lane] = cnt;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t sum = 0;
+    for (int j = 0; j < 8; ++j) sum += wc[j][threadIdx.x];
+    const uint32_t c = w * 32 + threadIdx.x;
+    counts[(uint64_t)c * T + t] = cuboid_wanted(c, nsub, max_d) ? sum : 0u;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_bits_write(
+    const uint32_t* __restrict__ bits, uint32_t W,
+    const uint32_t* __restrict__ m_ptr, uint32_t T, int count_set,
+    uint32_t nsub, int max_d, const uint64_t* __restrict__ offs,
+    const uint32_t* __restrict__ cand, uint32_t* __restrict__ out) {
+  __shared__ uint32_t wc[8][32];
+  __shared__ uint32_t run[8][32];
+  const uint32_t t = blockIdx.x, w = blockIdx.y;
+  const int lane = threadIdx.x & 31, k = threadIdx.x >> 5;
+  const uint32_t m = *m_ptr;
+  if (t * kTileRows >= m) return;  // uniform over the CTA
+  const uint32_t row0 = t * kTileRows + k * 256;
+  // pass 1: per-warp counts
+  uint32_t cnt = 0;
+  for (int s = 0; s < 8; ++s) {
+    const uint32_t v = counted_bits(bits, W, row0 + s * 32 + lane, m, w, count_set);
+#pragma unroll
+    for (int b = 0; b < 32; ++b) {
+      const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
+      if (lane == b) cnt += __popc(bal);
+    }
+  }
+  wc[k][lane] = cnt;
+  __syncthreads();
+  // exclusive prefix over warps, per bit
+  if (threadIdx.x < 32) {
+    uint32_t acc = 0;
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t v = wc[j][threadIdx.x];
+      run[j][threadIdx.x] = acc;
+      acc += v;
+    }
+  }
+  __syncthreads();
+  // pass 2: write ids
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  for (int s = 0; s < 8; ++s) {
+    const uint32_t r = row0 + s * 32 + lane;
+    const uint32_t v = counted_bits(bits, W, r, m, w, count_set);
+    const uint32_t id = r < m ? cand[r] : 0u;
+#pragma unroll 4
+    for (int b = 0; b < 32; ++b) {
+      const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
+      if (!bal) continue;
+      const uint32_t c = w * 32 + b;
+      if (!cuboid_wanted(c, nsub, max_d)) continue;
+      const uint32_t base = run[k][b];
+      if ((v >> b) & 1u)
+        out[offs[(uint64_t)c * T + t] + base + __popc(bal & lt_mask)] = id;
+      __syncwarp();
+      if (lane == 0) run[k][b] = base + __popc(bal);
+      __syncwarp();
+    }
+  }
+}
+
+// csr_off[c] = offs[c * T] for c in [0, nsub]; offs[32*W*T] is the total.
+__global__ void k_extract_csr(const uint64_t* __restrict__ offs, uint32_t T,
+                              uint32_t nsub, uint64_t* __restrict__ csr_off) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c <= nsub;
+       c += gridDim.x * blockDim.x)
+    csr_off[c] = offs[(uint64_t)c * T];
+}
+
+int launch_bits_count(cudaStream_t s, const CompactArgs& a) {
+  const uint32_t T = compact_tiles(a.m_max);
+  const uint64_t C = 32ull * a.words;
+  k_bits_count<<<dim3(T, a.words), 256, 0, s>>>(a.bits, a.words, a.m_ptr, T, a.count_set,
+                                                 a.nsub, a.max_d, a.counts);
+  SKC_LAUNCH_CHECK();
+  SKC_TRY(launch_scan_u32_to_u64(s, a.counts, C * T, a.bsum, a.offs));
+  k_extract_csr<<<(a.nsub + 256) / 256, 256, 0, s>>>(a.offs, T, a.nsub, a.csr_off);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
+int launch_bits_write(cudaStream_t s, const CompactArgs& a) {
+  const uint32_t T = compact_tiles(a.m_max);
+  k_bits_write<<<dim3(T, a.words), 256, 0, s>>>(a.bits, a.words, a.m_ptr, T, a.count_set,
+                                                 a.nsub, a.max_d, a.offs, a.cand, a.out);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
+}  // namespace skc

@@ -1,0 +1,246 @@
+"""Python binding of the GB300 skycube engine's C ABI (include/skycube_gb300.h).
+
+The engine itself is CUDA + C++ (``libskycube_gb300.so``); this module is a
+thin ctypes layer used by the tests and the benchmark. It never computes a
+skycube in Python and raises ``SkycubeError`` if the native library is
+missing or a call fails.
+
+Vocabulary follows the skycube suite: a *cuboid* is a non-empty subspace,
+given as a bitmask over the d attributes; its *skyline* holds the point ids
+(row indices) no other point dominates on it, its *extended skyline* the
+dominated points nobody strictly dominates. ``algo`` is "mdmc" or "sdsc"
+(the suite's ``-s``), ``mode`` "plain" (one launch sequence per cuboid) or
+"batched" (one persistent launch for all cuboids), ``max_d`` the suite's
+``-m`` cap and ``depth`` its ``-d`` grid depth.
+"""
+import ctypes
+import os
+import weakref
+
+import numpy as np
+
+from .build import LIB_PATH, build  # noqa: F401
+
+SKC_OK = 0
+ERROR_NAMES = {1: "INVALID", 2: "CUDA", 3: "OOM", 4: "TIMEOUT", 5: "UNSUPPORTED", 6: "REJECTED"}
+ALGOS = {"mdmc": 0, "sdsc": 1}
+MODES = {"plain": 0, "batched": 1}
+
+
+class SkycubeError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"skycube error {ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [("algo", ctypes.c_int), ("mode", ctypes.c_int), ("max_d", ctypes.c_int),
+                ("depth", ctypes.c_int), ("want_extended", ctypes.c_int),
+                ("want_bitmaps", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libskycube_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise SkycubeError(2, f"native library {LIB_PATH} is missing; run skycube_gb300.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, u32, u64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+    P = ctypes.POINTER
+    sig = {
+        "skc_options_init": (None, [P(_Options)]),
+        "skc_context_create": (i32, [i32, P(vp)]),
+        "skc_context_destroy": (i32, [vp]),
+        "skc_dataset_upload": (i32, [vp, vp, u64, i32, P(vp)]),
+        "skc_dataset_upload_device": (i32, [vp, vp, u64, i32, P(vp)]),
+        "skc_dataset_free": (i32, [vp]),
+        "skc_skycube": (i32, [vp, vp, P(_Options), P(vp)]),
+        "skc_result_info": (i32, [vp, P(i32), P(u64), P(u64)]),
+        "skc_result_cuboid": (i32, [vp, u32, P(P(u32)), P(u64)]),
+        "skc_result_extended": (i32, [vp, u32, P(P(u32)), P(u64)]),
+        "skc_result_device_csr": (i32, [vp, P(vp), P(vp)]),
+        "skc_result_download": (i32, [vp]),
+        "skc_result_bitmaps": (i32, [vp, P(P(u32)), P(P(u32)), P(u64), P(u32)]),
+        "skc_result_free": (i32, [vp]),
+        "skc_last_device_ms": (i32, [vp, P(ctypes.c_float)]),
+        "skc_last_error": (ctypes.c_char_p, []),
+        "skc_kernel_launches": (u64, []),
+        "skc_last_phase": (i32, [vp, i32, P(ctypes.c_char_p), P(ctypes.c_float)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(code):
+    if code != SKC_OK:
+        raise SkycubeError(code, lib().skc_last_error().decode())
+
+
+class Context:
+    """A CUDA device plus the engine's stream and memory pool (the -g value)."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        _check(lib().skc_context_create(device, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+        self._children = weakref.WeakSet()
+
+    def _adopt(self, child):
+        self._children.add(child)
+
+    def close(self):
+        if self.handle:
+            for c in list(self._children):
+                c.close()
+            lib().skc_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_phases(self):
+        """[(phase name, device ms)] of the last skycube call."""
+        out, i = [], 0
+        name, ms = ctypes.c_char_p(), ctypes.c_float()
+        while lib().skc_last_phase(self.handle, i, ctypes.byref(name), ctypes.byref(ms)) == SKC_OK:
+            out.append((name.value.decode(), ms.value))
+            i += 1
+        return out
+
+    def last_device_ms(self):
+        v = ctypes.c_float()
+        _check(lib().skc_last_device_ms(self.handle, ctypes.byref(v)))
+        return v.value
+
+
+class Dataset:
+    """A point set resident on the device (MDMC<D>::Init / SDSC<D>::Init)."""
+
+    def __init__(self, ctx, points=None, device_ptr=None, n=None, d=None):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        if device_ptr is not None:
+            _check(lib().skc_dataset_upload_device(ctx.handle, ctypes.c_void_p(device_ptr),
+                                                   n, d, ctypes.byref(h)))
+            self.n, self.d = n, d
+        else:
+            x = np.ascontiguousarray(points, dtype=np.float32)
+            if x.ndim != 2:
+                raise SkycubeError(1, "points must be a 2-d array (n, d)")
+            self.n, self.d = x.shape
+            _check(lib().skc_dataset_upload(ctx.handle, x.ctypes.data_as(ctypes.c_void_p),
+                                            self.n, self.d, ctypes.byref(h)))
+        self.handle = h
+        ctx._adopt(self)
+
+    def close(self):
+        if self.handle:
+            lib().skc_dataset_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Result:
+    """Per-cuboid skylines (and optionally extended skylines / bitmaps)."""
+
+    def __init__(self, ctx, handle, d, max_d):
+        self.ctx = ctx  # keeps the context alive while the result is
+        self.handle = handle
+        self.d = d
+        self.max_d = max_d
+        ctx._adopt(self)
+
+    def close(self):
+        if self.handle:
+            lib().skc_result_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        d, m, t = ctypes.c_int(), ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib().skc_result_info(self.handle, ctypes.byref(d), ctypes.byref(m), ctypes.byref(t)))
+        return {"d": d.value, "n_candidates": m.value, "total_skyline_ids": t.value}
+
+    def download(self):
+        _check(lib().skc_result_download(self.handle))
+
+    def _view(self, fn, cuboid):
+        p = ctypes.POINTER(ctypes.c_uint32)()
+        c = ctypes.c_uint64()
+        _check(fn(self.handle, cuboid, ctypes.byref(p), ctypes.byref(c)))
+        if c.value == 0:
+            return np.empty(0, dtype=np.uint32)
+        return np.ctypeslib.as_array(p, shape=(c.value,)).copy()
+
+    def cuboid(self, cuboid):
+        """Skyline ids of one cuboid (ascending)."""
+        return self._view(lib().skc_result_cuboid, cuboid)
+
+    def extended(self, cuboid):
+        """Extended-skyline ids of one cuboid (ascending)."""
+        return self._view(lib().skc_result_extended, cuboid)
+
+    def all_cuboids(self, extended=False):
+        """{cuboid mask: ids} for every cuboid within max_d."""
+        out = {}
+        for c in range(1, 1 << self.d):
+            if bin(c).count("1") <= self.max_d:
+                out[c] = self.extended(c) if extended else self.cuboid(c)
+        return out
+
+    def device_csr(self):
+        off, ids = ctypes.c_void_p(), ctypes.c_void_p()
+        _check(lib().skc_result_device_csr(self.handle, ctypes.byref(off), ctypes.byref(ids)))
+        return off.value, ids.value
+
+    def bitmaps(self):
+        """(bits[n_cand, words] uint32, pids[n_cand]) of the dominated subspaces."""
+        b = ctypes.POINTER(ctypes.c_uint32)()
+        p = ctypes.POINTER(ctypes.c_uint32)()
+        n, w = ctypes.c_uint64(), ctypes.c_uint32()
+        _check(lib().skc_result_bitmaps(self.handle, ctypes.byref(b), ctypes.byref(p),
+                                        ctypes.byref(n), ctypes.byref(w)))
+        if n.value == 0:
+            return np.zeros((0, w.value), np.uint32), np.zeros(0, np.uint32)
+        bits = np.ctypeslib.as_array(b, shape=(n.value * w.value,)).reshape(n.value, w.value).copy()
+        pids = np.ctypeslib.as_array(p, shape=(n.value,)).copy()
+        return bits, pids
+
+
+def kernel_launches():
+    """Kernels launched by the native library in this process so far."""
+    return int(lib().skc_kernel_launches())
+
+
+def skycube(ctx, ds, algo="mdmc", mode="batched", max_d=0, depth=0,
+            want_extended=False, want_bitmaps=False):
+    """Computes the skycube of a resident dataset (MDMC/SDSC ::Execute)."""
+    o = _Options(ALGOS[algo], MODES[mode], int(max_d), int(depth),
+                 int(bool(want_extended)), int(bool(want_bitmaps)))
+    h = ctypes.c_void_p()
+    _check(lib().skc_skycube(ctx.handle, ds.handle, ctypes.byref(o), ctypes.byref(h)))
+    md = ds.d if max_d <= 0 or max_d > ds.d else max_d
+    return Result(ctx, h, ds.d, md)

@@ -1,0 +1,78 @@
+"""Seeded synthetic point sets with the shapes and value distributions of the
+benchmark workloads of the skycube suite (its own data files are not shipped).
+
+Every generator returns a C-contiguous float32 array of shape (n, d), rows are
+points and smaller is better on every attribute. All randomness comes from
+``numpy.random.default_rng(seed)`` so the same seed gives the same points.
+
+Distributions:
+  uniform         every coordinate iid U[0,1)
+  anticorrelated  v ~ N(0.5, sigma); x_i ~ U[0,1); every coordinate shifted by
+                  (d*v - sum x)/d; the point is redrawn if a coordinate leaves
+                  [0,1]
+  correlated      v ~ N(0.5, 0.25) clipped to [0,1]; x_i = clip(v + N(0,0.05))
+  ties            60% uniform, 40% correlated points, then floor(256*u) stored
+                  as float32 (integer valued, many duplicates)
+  correlated_q    correlated, rounded to multiples of 0.1/d of the unit range
+"""
+import numpy as np
+
+KINDS = ("uniform", "anticorrelated", "correlated", "ties", "correlated_q")
+
+
+def _uniform(rng, n, d):
+    return rng.random((n, d), dtype=np.float64)
+
+
+def _anticorrelated(rng, n, d, sigma=0.05):
+    out = np.empty((n, d), dtype=np.float64)
+    filled = 0
+    while filled < n:
+        m = max(1024, int((n - filled) * 1.3))
+        v = rng.normal(0.5, sigma, size=(m, 1))
+        x = rng.random((m, d))
+        x += (d * v - x.sum(axis=1, keepdims=True)) / d
+        ok = np.all((x >= 0.0) & (x <= 1.0), axis=1)
+        x = x[ok]
+        take = min(len(x), n - filled)
+        out[filled:filled + take] = x[:take]
+        filled += take
+    return out
+
+
+def _correlated(rng, n, d):
+    v = np.clip(rng.normal(0.5, 0.25, size=(n, 1)), 0.0, 1.0)
+    return np.clip(v + rng.normal(0.0, 0.05, size=(n, d)), 0.0, 1.0)
+
+
+def generate(kind, n, d, seed=1):
+    """Returns an (n, d) float32 point set of the given distribution."""
+    if kind not in KINDS:
+        raise ValueError(f"unknown distribution {kind!r}; expected one of {KINDS}")
+    rng = np.random.default_rng(seed)
+    if kind == "uniform":
+        x = _uniform(rng, n, d)
+    elif kind == "anticorrelated":
+        x = _anticorrelated(rng, n, d)
+    elif kind == "correlated":
+        x = _correlated(rng, n, d)
+    elif kind == "ties":
+        n_corr = (n * 4) // 10
+        u = _uniform(rng, n - n_corr, d)
+        c = _correlated(rng, n_corr, d)
+        x = np.concatenate([u, c], axis=0)
+        x = x[rng.permutation(n)]
+        x = np.floor(256.0 * x)
+    else:  # correlated_q
+        step = 0.1 / d
+        x = np.round(_correlated(rng, n, d) / step) * step
+    return np.ascontiguousarray(x, dtype=np.float32)
+
+
+# The five benchmark workloads: (distribution, n, d, max_d, seed).
+CONFIGS = {
+    "uniform-100k-6": ("uniform", 100_000, 6, 6, 1),
+    "anticorr-1m-10": ("anticorrelated", 1_000_000, 10, 10, 1),
+    "ties-581k-10": ("ties", 581_012, 10, 10, 42),
+    "corrq-566k-15-m6": ("correlated_q", 566_268, 15, 6, 42),
+}

@@ -1,0 +1,87 @@
+"""Generates the golden fixtures of tests/golden from the REFERENCE's own STSC.
+
+Runs only where the reference checkout is present and oracle/build_ref.sh has
+built oracle/_ref/libskycube_ref.so (the reference's HybridCube + MommyQ
+compiled from its sources). For every case it stores the input points and the
+reference's per-cuboid skyline and extended-skyline id sets, so the fixtures
+pin both the C oracle and the CUDA path on machines without the reference.
+
+Usage: python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "skycube-templates_gb300"))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+from skycube_gb300 import datagen  # noqa: E402
+import oracle  # noqa: E402
+
+# name: (distribution, n, d, max_d, seed)
+CASES = {
+    "uniform_2000_6": ("uniform", 2000, 6, 6, 1),
+    "ties_3000_6": ("ties", 3000, 6, 6, 2),
+    "anticorr_2000_8": ("anticorrelated", 2000, 8, 8, 3),
+    "corrq_2000_10_m4": ("correlated_q", 2000, 10, 4, 4),
+    "ties_1500_12_m3": ("ties", 1500, 12, 3, 5),
+    "uniform_400_16_m2": ("uniform", 400, 16, 2, 6),
+    "anticorr_3000_5": ("anticorrelated", 3000, 5, 5, 7),
+    "ties_800_2": ("ties", 800, 2, 2, 8),
+}
+
+
+def edge_cases():
+    """Small hand-made inputs: duplicates, a single point, signed zeros."""
+    rng = np.random.default_rng(99)
+    dup = np.repeat(rng.random((5, 4), dtype=np.float64), 7, axis=0)
+    dup = dup[rng.permutation(len(dup))].astype(np.float32)
+    same = np.full((40, 3), 0.5, dtype=np.float32)
+    one = np.array([[0.25, 0.75, 0.5]], dtype=np.float32)
+    zeros = np.array([[0.0, 1.0], [-0.0, 1.0], [0.0, 0.5], [1.0, -0.0], [-0.0, 0.0]],
+                     dtype=np.float32)
+    grid = np.floor(rng.random((600, 7)) * 3).astype(np.float32)  # 3 levels: heavy ties
+    return {
+        "edge_duplicates_35_4": (dup, 4),
+        "edge_identical_40_3": (same, 3),
+        "edge_single_1_3": (one, 3),
+        "edge_signed_zero_5_2": (zeros, 2),
+        "edge_grid3_600_7": (grid, 7),
+    }
+
+
+def pack(d, sets):
+    off = [0]
+    ids = []
+    for c in range(1, 1 << d):
+        a = sets.get(c, np.empty(0, np.uint32))
+        ids.append(a)
+        off.append(off[-1] + len(a))
+    return np.array(off, np.uint64), (np.concatenate(ids) if ids else np.empty(0, np.uint32)).astype(np.uint32)
+
+
+def write(name, x, max_d):
+    d = x.shape[1]
+    res = oracle.ref_stsc(x, max_d, threads=8)
+    if res is None:
+        raise SystemExit("reference STSC not built: run oracle/build_ref.sh first")
+    sky, ext = res
+    so, si = pack(d, sky)
+    eo, ei = pack(d, ext)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), x=x, max_d=np.int32(max_d),
+                        sky_off=so, sky_ids=si, ext_off=eo, ext_ids=ei)
+    print(f"{name}: n={len(x)} d={d} max_d={max_d} skyline ids={len(si)} extended ids={len(ei)}")
+
+
+def main():
+    for name, (kind, n, d, max_d, seed) in CASES.items():
+        write(name, datagen.generate(kind, n, d, seed), max_d)
+    for name, (x, d) in edge_cases().items():
+        write(name, x, d)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,63 @@
+"""The CPU oracle pinned against the reference: golden fixtures produced by
+the reference's own STSC, definition-level brute force, and (where the
+reference was built in this checkout) a live comparison."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden_names, load_golden, wanted
+from skycube_gb300 import datagen
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_matches_reference_golden(name):
+    x, max_d, sky, ext = load_golden(name)
+    d = x.shape[1]
+    osky, oext = oracle.stsc(x, max_d)
+    for c in range(1, 1 << d):
+        if not wanted(c, d, max_d):
+            continue
+        assert np.array_equal(osky[c], sky[c]), f"skyline of cuboid {c}"
+        assert np.array_equal(oext[c], ext[c]), f"extended skyline of cuboid {c}"
+
+
+def _random_points(rng, n, d, levels):
+    if levels:
+        return np.floor(rng.random((n, d)) * levels).astype(np.float32)
+    return rng.random((n, d), dtype=np.float64).astype(np.float32)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_oracle_matches_bruteforce(seed):
+    rng = np.random.default_rng(1000 + seed)
+    d = int(rng.integers(2, 7))
+    n = int(rng.integers(1, 70))
+    levels = [0, 2, 3, 8][seed % 4]
+    x = _random_points(rng, n, d, levels)
+    bits = oracle.bruteforce_bitmaps(x)
+    truth = oracle.skylines_from_bitmaps(bits, d)
+    sky, _ = oracle.stsc(x)
+    for c in range(1, 1 << d):
+        assert np.array_equal(sky[c], truth[c]), f"cuboid {c}"
+
+
+def test_bruteforce_definition_tiny():
+    # q=(0,1) vs p=(0,2): q dominates p on {1} and {0,1}, not on {0} (tie).
+    x = np.array([[0.0, 2.0], [0.0, 1.0]], dtype=np.float32)
+    bits = oracle.bruteforce_bitmaps(x)
+    assert bits[0, 0] == (1 << 2) | (1 << 3)
+    assert bits[1, 0] == 0
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference STSC not built here")
+@pytest.mark.parametrize("kind,n,d,max_d,seed", [
+    ("uniform", 5000, 7, 7, 11), ("ties", 6000, 9, 9, 12), ("correlated_q", 4000, 13, 3, 13),
+    ("anticorrelated", 4000, 6, 6, 14), ("correlated", 3000, 11, 11, 15),
+])
+def test_oracle_matches_reference_live(kind, n, d, max_d, seed):
+    x = datagen.generate(kind, n, d, seed)
+    a = oracle.ref_stsc(x, max_d)
+    b = oracle.stsc(x, max_d)
+    for c in a[0]:
+        assert np.array_equal(a[0][c], b[0][c])
+        assert np.array_equal(a[1][c], b[1][c])
