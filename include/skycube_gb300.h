@@ -145,6 +145,28 @@ int skc_last_phase(skc_context* ctx, int index, const char** name, float* ms);
  * contexts). A caller brackets a region with two reads to count launches. */
 uint64_t skc_kernel_launches(void);
 
+/* Allocation-free skyline of one subspace, for callers that cannot allocate
+ * device memory (for example a host process whose own allocator already owns
+ * the GPU's memory, or a plugin that may not touch the device heap). No
+ * counterpart in the reference: it is an addition of this library.
+ *
+ * d_rows: n x d row-major float32 points in DEVICE memory; d_status: n bytes
+ * of DEVICE memory that receive, per point, 0 (skyline of `subspace`),
+ * 1 (extended skyline: dominated, never strictly) or 2 (strictly dominated).
+ * depth: grid depth 1..7, 0 for the default. stream: a cudaStream_t (NULL for
+ * the default stream); the call returns after the statuses are written.
+ *
+ * Limits: n <= 65536 points, 2 <= d <= 16. Larger inputs are rejected with
+ * SKC_ERR_UNSUPPORTED before any device work. All temporaries live in one
+ * static device array of about 6.3 MiB inside the library, held by every GPU
+ * that loads it until the process exits; the call makes no allocation. The
+ * first call on a device resolves that array's address (make it before any
+ * stream capture). Calls share the array, so calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+int skc_skyline_noalloc(const float* d_rows, uint32_t n, int d,
+                        uint32_t subspace, int depth, uint8_t* d_status,
+                        void* stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* skc_last_error(void);
 
