@@ -142,6 +142,56 @@ static int rank_table(skc_context* ctx, int d, const uint32_t** out) {
   return SKC_OK;
 }
 
+// Partition tables over B-bit masks, built once per context (partition.cu):
+// one device buffer [rank | unrank | sub_off | sub_list].
+static int level_tables(skc_context* ctx, int B, LevelTables* out) {
+  const uint32_t ns = 1u << B;
+  if (!ctx->d_level_tables[B]) {
+    std::vector<uint32_t> order(ns), rank(ns);
+    for (uint32_t i = 0; i < ns; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [](uint32_t a, uint32_t b) {
+      return __builtin_popcount(a) < __builtin_popcount(b);
+    });
+    for (uint32_t i = 0; i < ns; ++i) rank[order[i]] = i;
+    std::vector<uint32_t> sub_off(ns + 1, 0), sub_list;
+    for (uint32_t mk = 0; mk < ns; ++mk) {
+      sub_off[mk] = (uint32_t)sub_list.size();
+      for (uint32_t r = 0; r < ns; ++r)
+        if ((order[r] & ~mk) == 0) sub_list.push_back(r);
+    }
+    sub_off[ns] = (uint32_t)sub_list.size();
+    std::vector<uint32_t> all;
+    all.insert(all.end(), rank.begin(), rank.end());
+    all.insert(all.end(), order.begin(), order.end());
+    all.insert(all.end(), sub_off.begin(), sub_off.end());
+    all.insert(all.end(), sub_list.begin(), sub_list.end());
+    uint32_t* p = nullptr;
+    SKC_CUDA(cudaMalloc(&p, all.size() * sizeof(uint32_t)));
+    SKC_CUDA(cudaMemcpy(p, all.data(), all.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    ctx->d_level_tables[B] = p;
+  }
+  uint32_t* p = ctx->d_level_tables[B];
+  out->B = B;
+  out->rank = p;
+  out->unrank = p + ns;
+  out->sub_off = p + 2 * ns;
+  out->sub_list = p + 3 * ns + 1;
+  return SKC_OK;
+}
+
+static int partition_dims(uint32_t S) {
+  const int k = __builtin_popcount(S);
+  return k < kMaxPartitionDims ? k : kMaxPartitionDims;
+}
+
+// Partition width of the bitmap kernel's q order: as many attributes as
+// keep partitions at >= 256 points on average (at most 10, at least 1).
+static int bitmap_partition_dims(int d, uint64_t m) {
+  int B = 1;
+  while (B < kMaxPartitionDims && B < d && (m >> (B + 1)) >= 256) ++B;
+  return B;
+}
+
 // Device-side result of the full-space step.
 struct FullSpace {
   uint4* cells = nullptr;    // by point id (depth of the call)
@@ -167,23 +217,21 @@ static int run_full_space(skc_context* ctx, skc_dataset* ds, int depth,
   SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, nullptr, d_n, n, depth, pivots, F.cells));
   T.mark("full: pivots+cells");
 
-  const uint32_t K = bucket_count(n);
-  BucketScratch b;
-  SKC_TRY(A.alloc(&b.f, n));
-  SKC_TRY(A.alloc(&b.keys, n));
-  SKC_TRY(A.alloc(&b.counts, K + 1));
-  SKC_TRY(A.alloc(&b.cursor, K + 1));
-  SKC_TRY(A.alloc(&b.minmax, 2));
-  uint32_t *sorted, *hi;
-  SKC_TRY(A.alloc(&sorted, n));
-  SKC_TRY(A.alloc(&hi, n));
-  SKC_TRY(launch_bucket_order(s, ds->x, ds->n_pad, d, nullptr, d_n, n, full, K, b, sorted, hi));
-  T.mark("full: norm order");
-
+  LevelTables LT;
+  SKC_TRY(level_tables(ctx, partition_dims(full), &LT));
+  const uint32_t K = 1u << LT.B;
+  PartScratch ps;
+  SKC_TRY(A.alloc(&ps.keys, n));
+  SKC_TRY(A.alloc(&ps.sorted, n));
+  SKC_TRY(A.alloc(&ps.ccells, n));
+  SKC_TRY(A.alloc(&ps.cx, (uint64_t)d * round_up(n, 128)));
+  SKC_TRY(A.alloc(&ps.counts, K + 1));
+  SKC_TRY(A.alloc(&ps.cursor, K + 1));
+  SKC_TRY(A.alloc(&ps.items, K + 1));
   uint8_t* status;
   SKC_TRY(A.alloc(&status, n));
-  SkylineArgs a{sorted, hi, nullptr, F.cells, ds->x, ds->n_pad, d_n, n, full, status};
-  SKC_TRY(launch_skyline(s, d, a));
+  PartitionSkylineArgs pa{nullptr, F.cells, ds->x, ds->n_pad, d_n, n, full, status};
+  SKC_TRY(launch_partition_skyline(s, d, depth, LT, pa, ps));
   T.mark("full: skyline kernel");
 
   const uint64_t nblk = (n + 1023) / 1024 + 1;
@@ -229,17 +277,20 @@ static int run_bitmaps(skc_context* ctx, skc_dataset* ds, const skc_options& o,
   SKC_TRY(A.alloc(&bmin, (m + 31) / 32));
   SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, F.cand, m_ptr, m, depth, pivots, cc));
 
-  const uint32_t* rank;
-  SKC_TRY(rank_table(ctx, d, &rank));
+  // q order: partitions by median mask over the first B attributes, in
+  // lattice-level order (strongest partitions first).
+  LevelTables LT;
+  SKC_TRY(level_tables(ctx, bitmap_partition_dims(d, m), &LT));
+  const uint32_t K = 1u << LT.B;
   BucketScratch b;
   SKC_TRY(A.alloc(&b.keys, m));
-  SKC_TRY(A.alloc(&b.counts, nsub + 1));
-  SKC_TRY(A.alloc(&b.cursor, nsub + 1));
+  SKC_TRY(A.alloc(&b.counts, K + 1));
+  SKC_TRY(A.alloc(&b.cursor, K + 1));
   uint32_t *qperm, *qids;
   SKC_TRY(A.alloc(&qperm, m));
   SKC_TRY(A.alloc(&qids, m));
-  SKC_TRY(launch_level_keys(s, cc, m_ptr, m, d, depth, rank, b.keys));
-  SKC_TRY(launch_counting_sort(s, b.keys, m_ptr, m, nsub, b, qperm, nullptr));
+  SKC_TRY(launch_mask_keys(s, cc, nullptr, m_ptr, m, nsub - 1, d, LT.B, depth, LT.rank, b.keys));
+  SKC_TRY(launch_counting_sort(s, b.keys, m_ptr, m, K, b, qperm, nullptr));
   SKC_TRY(launch_gather_u32(s, F.cand, qperm, m_ptr, m, qids));
   SKC_TRY(launch_gather_soa(s, ds->x, ds->n_pad, d, qids, m_ptr, m, m_pad, xq));
   SKC_TRY(launch_gather_u4(s, cc, qperm, m_ptr, m, qc));
@@ -251,7 +302,8 @@ static int run_bitmaps(skc_context* ctx, skc_dataset* ds, const skc_options& o,
   if (want_ext) SKC_TRY(A.alloc(&ext, m * W));
   SKC_TRY(A.alloc(&work, 1));
 
-  BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, m_ptr, work, 0xffffffffu, dom, ext, 0};
+  BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, b.counts, LT.unrank, K, LT.B, depth,
+                m_ptr, work, 0xffffffffu, dom, ext, 0};
   if (o.mode == SKC_MODE_BATCHED) {
     SKC_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), s));
     SKC_TRY(launch_bitmaps(s, d, ctx->num_sms, ba));
@@ -331,7 +383,8 @@ static int run_bitmaps(skc_context* ctx, skc_dataset* ds, const skc_options& o,
 
 // The suite's per-cuboid schedule (PLAIN/SDSC).
 static int run_sdsc_plain(skc_context* ctx, skc_dataset* ds, int max_d,
-                          Arena& A, FullSpace& F, skc_result* R, Tracer& T) {
+                          int depth_of_call, Arena& A, FullSpace& F,
+                          skc_result* R, Tracer& T) {
   cudaStream_t s = ctx->stream;
   const int d = ds->d;
   const uint32_t nsub = 1u << d, full = nsub - 1;
@@ -343,17 +396,17 @@ static int run_sdsc_plain(skc_context* ctx, skc_dataset* ds, int max_d,
   next[full] = F.h_counts[1];
 
   uint64_t mmax = nsky[full] + next[full];
-  const uint32_t K = bucket_count(mmax);
-  BucketScratch b;
-  SKC_TRY(A.alloc(&b.f, mmax));
-  SKC_TRY(A.alloc(&b.keys, mmax));
-  SKC_TRY(A.alloc(&b.counts, K + 1));
-  SKC_TRY(A.alloc(&b.cursor, K + 1));
-  SKC_TRY(A.alloc(&b.minmax, 2));
-  uint32_t *sorted, *hi, *cand, *d_m, *blk0, *blk1, *cnt;
+  PartScratch ps;
+  const uint32_t Kmax = 1u << kMaxPartitionDims;
+  SKC_TRY(A.alloc(&ps.keys, mmax));
+  SKC_TRY(A.alloc(&ps.sorted, mmax));
+  SKC_TRY(A.alloc(&ps.ccells, mmax));
+  SKC_TRY(A.alloc(&ps.cx, (uint64_t)d * round_up(mmax, 128)));
+  SKC_TRY(A.alloc(&ps.counts, Kmax + 1));
+  SKC_TRY(A.alloc(&ps.cursor, Kmax + 1));
+  SKC_TRY(A.alloc(&ps.items, Kmax + 1));
+  uint32_t *cand, *d_m, *blk0, *blk1, *cnt;
   uint8_t* status;
-  SKC_TRY(A.alloc(&sorted, mmax));
-  SKC_TRY(A.alloc(&hi, mmax));
   SKC_TRY(A.alloc(&cand, mmax));
   SKC_TRY(A.alloc(&status, mmax));
   SKC_TRY(A.alloc(&d_m, 1));
@@ -391,9 +444,10 @@ static int run_sdsc_plain(skc_context* ctx, skc_dataset* ds, int max_d,
       if ((st = launch_merge_disjoint(s, sky[src], (uint32_t)nsky[src], ext[src], (uint32_t)next[src], cand)) != SKC_OK) break;
       cudaError_t e = cudaSuccess;
       if ((st = launch_set_u32(s, d_m, (uint32_t)mc)) != SKC_OK) break;
-      if ((st = launch_bucket_order(s, ds->x, ds->n_pad, d, cand, d_m, mc, c, bucket_count(mc), b, sorted, hi)) != SKC_OK) break;
-      SkylineArgs a{sorted, hi, cand, F.cells, ds->x, ds->n_pad, d_m, mc, c, status};
-      if ((st = launch_skyline(s, d, a)) != SKC_OK) break;
+      LevelTables LT;
+      if ((st = level_tables(ctx, partition_dims(c), &LT)) != SKC_OK) break;
+      PartitionSkylineArgs pa{cand, F.cells, ds->x, ds->n_pad, d_m, mc, c, status};
+      if ((st = launch_partition_skyline(s, d, depth_of_call, LT, pa, ps)) != SKC_OK) break;
       uint32_t *osky, *oext;
       if ((st = A.alloc(&osky, mc)) != SKC_OK) break;
       if ((st = A.alloc(&oext, mc)) != SKC_OK) break;
@@ -551,6 +605,8 @@ int skc_context_destroy(skc_context* ctx) {
   cudaStreamSynchronize(ctx->stream);
   for (auto* p : ctx->d_rank_tables)
     if (p) cudaFree(p);
+  for (auto* p : ctx->d_level_tables)
+    if (p) cudaFree(p);
   cudaEventDestroy(ctx->ev_start);
   cudaEventDestroy(ctx->ev_stop);
   cudaStreamDestroy(ctx->stream);
@@ -666,7 +722,7 @@ int skc_skycube(skc_context* ctx, skc_dataset* ds, const skc_options* opt, skc_r
       if (o.algo == SKC_ALGO_SDSC && o.mode == SKC_MODE_PLAIN) {
         A.release(F.sky);
         A.release(F.ext);
-        st = run_sdsc_plain(ctx, ds, max_d, A, F, R, T);
+        st = run_sdsc_plain(ctx, ds, max_d, depth, A, F, R, T);
         cudaFreeAsync(F.sky, s);
         cudaFreeAsync(F.ext, s);
       } else {

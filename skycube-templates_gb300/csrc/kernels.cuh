@@ -35,6 +35,7 @@ int launch_status_compact(cudaStream_t s, const uint8_t* st, const uint32_t* ids
                           const uint32_t* m_ptr, uint64_t m_max, int merge01,
                           uint32_t* blk0, uint32_t* blk1, uint32_t* out0,
                           uint32_t* out1, uint32_t* n0, uint32_t* n1);
+int launch_scan_single_u32(cudaStream_t s, uint32_t* a, uint32_t len);
 int launch_scan_u32_to_u64(cudaStream_t s, const uint32_t* in, uint64_t len,
                            uint64_t* bsum, uint64_t* out);
 uint64_t scan_bsum_entries(uint64_t len);
@@ -75,6 +76,44 @@ struct SkylineArgs {
 };
 int launch_skyline(cudaStream_t s, int d, const SkylineArgs& a);
 
+// partition.cu: median-partition skyline (status as above).
+// Lattice-level tables over B-bit masks (B <= 10): rank (popcount, then
+// value), its inverse, and for every mask the ranks of its submasks in
+// level order.
+constexpr int kMaxPartitionDims = 10;
+struct LevelTables {
+  int B = 0;
+  const uint32_t* rank = nullptr;      // [2^B]
+  const uint32_t* unrank = nullptr;    // [2^B]
+  const uint32_t* sub_off = nullptr;   // [2^B + 1]
+  const uint32_t* sub_list = nullptr;  // [3^B]
+};
+struct PartScratch {
+  uint32_t* keys;    // [m_max]
+  uint32_t* sorted;  // [m_max]
+  uint4* ccells;     // [m_max] compact cells in partition order
+  float* cx;         // [|S| * round_up(m_max, 128)] compact floats
+  uint32_t* counts;  // [2^B + 1] partition offsets after the sort
+  uint32_t* cursor;  // [2^B + 1]
+  uint32_t* items;   // [2^B + 1]
+};
+struct PartitionSkylineArgs {
+  const uint32_t* ids;  // list position -> point id (nullptr: identity)
+  const uint4* cells;   // point id -> grid cells
+  const float* x;
+  uint64_t n_pad;
+  const uint32_t* m_ptr;
+  uint64_t m_max;
+  uint32_t S;
+  uint8_t* status;      // list position -> status
+};
+int launch_mask_keys(cudaStream_t s, const uint4* cells, const uint32_t* ids,
+                     const uint32_t* m_ptr, uint64_t m_max, uint32_t S, int d,
+                     int B, int depth, const uint32_t* rank, uint32_t* keys);
+int launch_partition_skyline(cudaStream_t s, int d, int depth,
+                             const LevelTables& T, const PartitionSkylineArgs& a,
+                             const PartScratch& ps);
+
 // mdmc.cu: per-point dominated-subspace bitmaps over the candidate set.
 struct BitmapArgs {
   const uint4* pcells;   // candidate order
@@ -83,6 +122,11 @@ struct BitmapArgs {
   const uint4* qcells;   // q order (level-sorted)
   const float* qx;       // q order, attribute-major, pitch p_pad
   const uint4* bmin;     // per block of 32 q's
+  const uint32_t* boff;  // q partitions: offsets in q order [K + 1]
+  const uint32_t* unrank;  // partition rank -> median mask over B attributes
+  uint32_t K;
+  int B;
+  int depth;
   const uint32_t* m_ptr;
   uint32_t* work;        // work counter, must hold p_begin
   uint32_t p_end;        // stop at min(m, p_end)

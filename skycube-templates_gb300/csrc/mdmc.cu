@@ -56,11 +56,44 @@ struct BitState {
   static constexpr bool REG = (W <= 32);
 };
 
+// Word w of down(L) is c_submask[L & 31] when w is a subset of L >> 5.
+// pdep_bits spreads the low bits of t over the set bits of mask: the t-th
+// subset of mask in increasing order.
+__device__ __forceinline__ uint32_t pdep_bits(uint32_t t, uint32_t mask) {
+  uint32_t w = 0;
+  while (mask) {
+    const uint32_t low = mask & (0u - mask);
+    if (t & 1u) w |= low;
+    t >>= 1;
+    mask &= mask - 1;
+  }
+  return w;
+}
+
+// Splits the subsets of h over 32 lanes: `low` = the lowest five set bits of
+// h, `rest` = the others. Lane j < 2^popc(low) gets base = the j-th subset
+// of low and walks every subset of rest; other lanes get nothing (false).
+__device__ __forceinline__ bool split_words(uint32_t h, int lane, uint32_t* base,
+                                            uint32_t* rest) {
+  uint32_t low = 0, t = h;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    low |= t & (0u - t);
+    t &= t - 1;
+  }
+  if ((uint32_t)lane >= (1u << __popc(low))) return false;
+  *base = pdep_bits((uint32_t)lane, low);
+  *rest = h ^ low;
+  return true;
+}
+
 template <int D>
 __global__ void __launch_bounds__(256) k_bitmaps(
     const uint4* __restrict__ pcells, const float* __restrict__ px,
     uint64_t p_pad, const uint4* __restrict__ qcells,
     const float* __restrict__ qx, const uint4* __restrict__ bmin,
+    const uint32_t* __restrict__ boff, const uint32_t* __restrict__ unrank,
+    uint32_t K, int B, int depth,
     const uint32_t* __restrict__ m_ptr, uint32_t* __restrict__ work,
     uint32_t p_end_cap, uint32_t* __restrict__ out_dom,
     uint32_t* __restrict__ out_ext) {
@@ -77,8 +110,8 @@ __global__ void __launch_bounds__(256) k_bitmaps(
   uint32_t* tie_s = REG ? nullptr : sat_s + W;
   const uint32_t m = *m_ptr;
   const uint32_t pend = min(m, p_end_cap);
-  const uint32_t nblk = (m + 31) / 32;
   const uint32_t wi = REG ? (uint32_t)lane % W : 0;
+  const int sh = depth - 1;
 
   for (;;) {
     uint32_t p = 0;
@@ -93,6 +126,11 @@ __global__ void __launch_bounds__(256) k_bitmaps(
       pc[w] = word_of(pc4, w);
       pH[w] = pc[w] | kGuard;
     }
+    // p's median mask over the partitioning attributes 0 .. B-1
+    uint32_t pmask = 0;
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+      if (k < B) pmask |= ((word_of(pc4, k >> 2) >> (8 * (k & 3) + sh)) & 1u) << k;
     float pv[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) pv[k] = px[(uint64_t)k * p_pad + p];
@@ -116,76 +154,121 @@ __global__ void __launch_bounds__(256) k_bitmaps(
       return (word >> (S & 31)) & 1u;
     };
 
-    for (uint32_t b = 0; b < nblk; ++b) {
-      const uint4 bm = bmin[b];
-      uint32_t Ub = 0;
-#pragma unroll
-      for (int w = 0; w < NW; ++w)
-        Ub |= pack_guards(ge_bytes(pH[w], word_of(bm, w))) << (4 * w);
-      Ub &= NSUB - 1;
-      if (in_strict(Ub)) continue;  // uniform: the whole block adds nothing
+    uint32_t next_blk = 0;  // blocks below this one were already visited
+    uint32_t lastE = 0xffffffffu, lastQ = 0;  // last tie update applied
+    for (uint32_t b = 0; b < K; ++b) {
+      const uint32_t qbeg = boff[b], qend = boff[b + 1];
+      if (qbeg == qend) continue;
+      // Attributes where every q of the partition is above the median and p
+      // is not: no q of it is <= p there. If the rest is already strict,
+      // the whole partition adds nothing.
+      const uint32_t X = unrank[b] & ~pmask;
+      if (in_strict((NSUB - 1) & ~X)) continue;
 
-      const uint32_t qi = b * 32 + lane;
-      const bool valid = qi < m;
-      uint4 q4 = make_uint4(0, 0, 0, 0);
-      if (valid) q4 = qcells[qi];
-      uint32_t U = 0;
-#pragma unroll
-      for (int w = 0; w < NW; ++w)
-        U |= pack_guards(ge_bytes(pH[w], word_of(q4, w))) << (4 * w);
-      U = valid ? (U & (NSUB - 1)) : 0u;
-      const bool hit = in_strict(U);
-      if (__all_sync(kFull, hit)) continue;
-
-      uint32_t le = 0, lt = 0;
-      if (!hit) {
-        uint32_t G = 0;  // cell(q) >= cell(p)
+      // A block shared with the previous partition is visited once; its q's
+      // from a skipped partition are tested too (any q's update is valid).
+      const uint32_t blk_end = (qend + 31) / 32;
+      uint32_t blk = max(qbeg / 32, next_blk);
+      next_blk = blk_end;
+      for (; blk < blk_end; ++blk) {
+        const uint4 bm = bmin[blk];
+        uint32_t Ub = 0;
 #pragma unroll
         for (int w = 0; w < NW; ++w)
-          G |= pack_guards(ge_bytes(word_of(q4, w) | kGuard, pc[w])) << (4 * w);
-        G &= NSUB - 1;
-        const uint32_t Y = U & ~G;  // certainly q < p
-        const uint32_t Z = U & G;   // equal cells: compare the floats
-        le = Y;
-        lt = Y;
-        if (Z) {
+          Ub |= pack_guards(ge_bytes(pH[w], word_of(bm, w))) << (4 * w);
+        Ub &= NSUB - 1;
+        if (in_strict(Ub)) continue;  // uniform: the whole block adds nothing
+
+        const uint32_t qi = blk * 32 + lane;
+        const bool valid = qi < m;
+        uint4 q4 = make_uint4(0, 0, 0, 0);
+        if (valid) q4 = qcells[qi];
+        uint32_t U = 0;
 #pragma unroll
-          for (int k = 0; k < D; ++k) {
-            if (Z & (1u << k)) {
-              const float a = qx[(uint64_t)k * p_pad + qi];
-              if (a <= pv[k]) le |= 1u << k;
-              if (a < pv[k]) lt |= 1u << k;
+        for (int w = 0; w < NW; ++w)
+          U |= pack_guards(ge_bytes(pH[w], word_of(q4, w))) << (4 * w);
+        U = valid ? (U & (NSUB - 1)) : 0u;
+        const bool hit = in_strict(U);
+        if (__all_sync(kFull, hit)) continue;
+
+        uint32_t le = 0, lt = 0;
+        if (!hit) {
+          uint32_t G = 0;  // cell(q) >= cell(p)
+#pragma unroll
+          for (int w = 0; w < NW; ++w)
+            G |= pack_guards(ge_bytes(word_of(q4, w) | kGuard, pc[w])) << (4 * w);
+          G &= NSUB - 1;
+          const uint32_t Y = U & ~G;  // certainly q < p
+          const uint32_t Z = U & G;   // equal cells: compare the floats
+          le = Y;
+          lt = Y;
+          if (Z) {
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+              if (Z & (1u << k)) {
+                const float a = qx[(uint64_t)k * p_pad + qi];
+                if (a <= pv[k]) le |= 1u << k;
+                if (a < pv[k]) lt |= 1u << k;
+              }
             }
           }
         }
-      }
-      const bool t_lt = in_strict(lt);
-      const bool t_le = in_strict(le);
-      const bool novel = !hit && (!t_lt || (le != lt && !t_le));
-      uint32_t todo = __ballot_sync(kFull, novel);
-      while (todo) {
-        const int src = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const uint32_t L = __shfl_sync(kFull, lt, src);
-        const uint32_t E = __shfl_sync(kFull, le, src);
-        const uint32_t Q = E & ~L;  // attributes with exact ties
-        if (REG) {
-          if ((wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
-          if (E != L && (wi & ~(E >> 5)) == 0) {
-            uint32_t mk = c_submask[E & 31];
-            if ((wi & ~(Q >> 5)) == 0) mk &= ~c_submask[Q & 31];
-            tie |= mk;
+        const bool t_lt = in_strict(lt);
+        const bool t_le = in_strict(le);
+        const bool novel = !hit && (!t_lt || (le != lt && !t_le));
+        uint32_t todo = __ballot_sync(kFull, novel);
+        while (todo) {
+          const int src = __ffs(todo) - 1;
+          todo &= todo - 1;
+          const uint32_t L = __shfl_sync(kFull, lt, src);
+          const uint32_t E = __shfl_sync(kFull, le, src);
+          // An earlier update may already cover this one.
+          const bool l_done = in_strict(L);
+          const uint32_t Q = E & ~L;  // attributes with exact ties
+          const bool e_done = (E == L) || in_strict(E) || (E == lastE && Q == lastQ);
+          if (l_done && e_done) continue;
+          if (E != L) {
+            lastE = E;
+            lastQ = Q;
           }
-        } else {
-          const uint32_t sl = c_submask[L & 31];
-          const uint32_t se = c_submask[E & 31];
-          const uint32_t sq = c_submask[Q & 31];
-          for (uint32_t w = lane; w < W; w += 32) {
-            if ((w & ~(L >> 5)) == 0) sat_s[w] |= sl;
-            if (E != L && (w & ~(E >> 5)) == 0)
-              tie_s[w] |= ((w & ~(Q >> 5)) == 0) ? (se & ~sq) : se;
+          if (REG) {
+            if (!l_done && (wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
+            if (!e_done && (wi & ~(E >> 5)) == 0) {
+              uint32_t mk = c_submask[E & 31];
+              if ((wi & ~(Q >> 5)) == 0) mk &= ~c_submask[Q & 31];
+              tie |= mk;
+            }
+          } else {
+            // Only the words under L (resp. E): the subsets of L >> 5. Lane
+            // j takes the j-th subset of the lowest five bits of L >> 5 and
+            // walks all subsets of the remaining bits.
+            if (!l_done) {
+              const uint32_t sl = c_submask[L & 31];
+              uint32_t base, rest;
+              if (split_words(L >> 5, lane, &base, &rest)) {
+                uint32_t sub = 0;
+                do {
+                  sat_s[base | sub] |= sl;
+                  sub = (sub - rest) & rest;
+                } while (sub);
+              }
+            }
+            if (!e_done) {
+              const uint32_t se = c_submask[E & 31];
+              const uint32_t sq = c_submask[Q & 31];
+              const uint32_t qh = Q >> 5;
+              uint32_t base, rest;
+              if (split_words(E >> 5, lane, &base, &rest)) {
+                uint32_t sub = 0;
+                do {
+                  const uint32_t w = base | sub;
+                  tie_s[w] |= ((w & ~qh) == 0) ? (se & ~sq) : se;
+                  sub = (sub - rest) & rest;
+                } while (sub);
+              }
+            }
+            __syncwarp();
           }
-          __syncwarp();
         }
       }
     }
@@ -233,8 +316,8 @@ static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
     grid = per_sm * num_sms;
   }
   k_bitmaps<D><<<grid, threads, smem, s>>>(a.pcells, a.px, a.p_pad, a.qcells, a.qx,
-                                           a.bmin, a.m_ptr, a.work, a.p_end,
-                                           a.out_dom, a.out_ext);
+                                           a.bmin, a.boff, a.unrank, a.K, a.B, a.depth,
+                                           a.m_ptr, a.work, a.p_end, a.out_dom, a.out_ext);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }

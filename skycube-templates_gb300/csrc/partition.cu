@@ -1,0 +1,263 @@
+// Median-partition skyline of a point list on one subspace S.
+//
+// Points are grouped by their median mask over the first B = min(|S|, 10)
+// attributes of S (bit j set when the point is worse than the median on that
+// attribute: the top bit of its grid cell). A point q can only dominate p
+// when q's mask is a subset of p's: on an attribute where q is above the
+// median and p is not, q is strictly worse. This is the partition test of
+// the suite's SkyAlign and Hybrid skylines (distribute_pitch_two_level_median,
+// src/utilities/kernels.cu:99-125; canskip_partition, src/utilities/
+// SubTuple.h:69-73), applied here to whole partitions at once.
+//
+// Layout. A counting sort groups the list by the lattice-level rank of the
+// mask (popcount, then value), so partitions of stronger points come first.
+// One CTA owns up to 256 points of ONE partition (a work item); it visits
+// only the partitions whose mask is a subset of its own, in level order, and
+// streams their points through shared memory 256 at a time. Each thread
+// tests its point against every staged point with the grid-cell SWAR test
+// and, when cells tie, exact float32 comparisons (see skyline.cu). A
+// strictly dominated point stops; the CTA stops when all its points have.
+#include "kernels.cuh"
+
+namespace skc {
+
+// key[i] = rank of the median mask of list entry i over the first B
+// attributes of S.
+__global__ void k_mask_keys(const uint4* __restrict__ cells,
+                            const uint32_t* __restrict__ ids,
+                            const uint32_t* __restrict__ m_ptr, uint32_t S,
+                            int d, int B, int depth,
+                            const uint32_t* __restrict__ rank,
+                            uint32_t* __restrict__ keys) {
+  const uint32_t m = *m_ptr;
+  const int sh = depth - 1;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += gridDim.x * blockDim.x) {
+    const uint32_t id = ids ? ids[i] : i;
+    const uint4 c = cells[id];
+    uint32_t cm = 0;
+    int j = 0;
+    for (int k = 0; k < d && j < B; ++k) {
+      if (!(S & (1u << k))) continue;
+      const uint32_t cell = (word_of(c, k >> 2) >> (8 * (k & 3))) & 0x7fu;
+      cm |= ((cell >> sh) & 1u) << j;
+      ++j;
+    }
+    keys[i] = rank[cm];
+  }
+}
+
+// items[b] = number of 256-point work items of partition b.
+__global__ void k_chunk_counts(const uint32_t* __restrict__ boff, uint32_t K,
+                               uint32_t* __restrict__ items) {
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < K;
+       b += gridDim.x * blockDim.x)
+    items[b] = (boff[b + 1] - boff[b] + 255) / 256;
+}
+
+// Compact copy of a list in partition order, restricted to the k attributes
+// of S: cells repacked so attribute t of S sits in byte t % 4 of word t / 4,
+// and attribute-major floats xs[t * pitch + j].
+__global__ void k_gather_compact(const uint4* __restrict__ cells,
+                                 const float* __restrict__ x, uint64_t n_pad,
+                                 const uint32_t* __restrict__ ids,
+                                 const uint32_t* __restrict__ sorted,
+                                 const uint32_t* __restrict__ m_ptr, uint32_t S,
+                                 int d, uint64_t pitch,
+                                 uint4* __restrict__ out_cells,
+                                 float* __restrict__ out_x) {
+  const uint32_t m = *m_ptr;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < m;
+       j += gridDim.x * blockDim.x) {
+    const uint32_t pos = sorted[j];
+    const uint32_t id = ids ? ids[pos] : pos;
+    const uint4 c = cells[id];
+    uint32_t w[4] = {0, 0, 0, 0};
+    int t = 0;
+    for (int k = 0; k < d; ++k) {
+      if (!(S & (1u << k))) continue;
+      const uint32_t cell = (word_of(c, k >> 2) >> (8 * (k & 3))) & 0x7fu;
+      w[t >> 2] |= cell << (8 * (t & 3));
+      out_x[(uint64_t)t * pitch + j] = x[(uint64_t)k * n_pad + id];
+      ++t;
+    }
+    out_cells[j] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+struct PartKernelArgs {
+  const uint32_t* sorted;   // sorted index -> list position (for the output)
+  const uint4* cells;       // compact cells in sorted order
+  const float* xs;          // compact floats in sorted order, pitch `pitch`
+  uint64_t pitch;
+  const uint32_t* boff;     // partition offsets in sorted order [K + 1]
+  const uint32_t* items;    // work item prefix per partition [K + 1]
+  const uint32_t* unrank;   // rank -> mask
+  const uint32_t* sub_off;  // mask -> range in sub_list
+  const uint32_t* sub_list; // ranks of submasks, level order
+  uint32_t K;
+  uint8_t* status;          // list position -> status
+};
+
+// NA = number of attributes of the subspace (all of them are compared).
+template <int NA>
+__global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
+  constexpr int NW = (NA + 3) / 4;
+  constexpr int TQ = 256;
+  __shared__ uint4 q_cells[TQ];
+  __shared__ float q_x[NA][TQ];
+
+  const uint32_t nitems = a.items[a.K];
+  if (blockIdx.x >= nitems) return;
+  const uint32_t it = nitems - 1 - blockIdx.x;  // heaviest partitions first
+  uint32_t lo = 0, hi = a.K;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a.items[mid] <= it) lo = mid; else hi = mid;
+  }
+  const uint32_t b = lo;
+  const uint32_t pbeg = a.boff[b] + (it - a.items[b]) * TQ;
+  const uint32_t pend = min(a.boff[b + 1], pbeg + TQ);
+  const uint32_t i = pbeg + threadIdx.x;
+  const bool valid = i < pend;
+
+  uint32_t hS[NW];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) hS[w] = guard_mask((1u << NA) - 1, w);
+  uint32_t pc[NW], pH[NW];
+  float pv[NA];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) pc[w] = pH[w] = 0;
+#pragma unroll
+  for (int k = 0; k < NA; ++k) pv[k] = 0.f;
+  if (valid) {
+    const uint4 c = a.cells[i];
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      pc[w] = word_of(c, w);
+      pH[w] = pc[w] | kGuard;
+    }
+#pragma unroll
+    for (int k = 0; k < NA; ++k) pv[k] = a.xs[(uint64_t)k * a.pitch + i];
+  }
+
+  uint8_t st = 0;
+  bool done = !valid;
+  bool all_done = false;
+  const uint32_t mb = a.unrank[b];
+  const uint32_t s1 = a.sub_off[mb + 1];
+  for (uint32_t si = a.sub_off[mb]; si < s1 && !all_done; ++si) {
+    const uint32_t qb = a.sub_list[si];
+    const uint32_t qend = a.boff[qb + 1];
+    for (uint32_t base = a.boff[qb]; base < qend; base += TQ) {
+      if (__syncthreads_and(done)) {
+        all_done = true;
+        break;
+      }
+      const uint32_t j = base + threadIdx.x;
+      if (j < qend) {
+        q_cells[threadIdx.x] = a.cells[j];
+#pragma unroll
+        for (int k = 0; k < NA; ++k) q_x[k][threadIdx.x] = a.xs[(uint64_t)k * a.pitch + j];
+      }
+      __syncthreads();
+      if (!done) {
+        const uint32_t lim = min((uint32_t)TQ, qend - base);
+        for (uint32_t t = 0; t < lim; ++t) {
+          const uint4 q = q_cells[t];
+          uint32_t worse = 0;  // guard bits where cell(q) > cell(p)
+#pragma unroll
+          for (int w = 0; w < NW; ++w) worse |= ~(pH[w] - word_of(q, w)) & hS[w];
+          if (worse) continue;
+          uint32_t not_less = 0;  // guard bits where cell(q) >= cell(p)
+#pragma unroll
+          for (int w = 0; w < NW; ++w)
+            not_less |= ge_bytes(word_of(q, w) | kGuard, pc[w]) & hS[w];
+          if (!not_less) {  // a smaller cell on every attribute: strict
+            st = 2;
+            done = true;
+            break;
+          }
+          bool le = true, lt_any = false, lt_all = true;
+#pragma unroll
+          for (int k = 0; k < NA; ++k) {
+            const float v = q_x[k][t];
+            le &= (v <= pv[k]);
+            lt_any |= (v < pv[k]);
+            lt_all &= (v < pv[k]);
+          }
+          if (le && lt_any) {
+            if (lt_all) {
+              st = 2;
+              done = true;
+              break;
+            }
+            st = 1;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (valid) a.status[a.sorted[i]] = st;
+}
+
+static inline unsigned blocks_for(uint64_t items, int threads, int cap);
+
+int launch_mask_keys(cudaStream_t s, const uint4* cells, const uint32_t* ids,
+                     const uint32_t* m_ptr, uint64_t m_max, uint32_t S, int d,
+                     int B, int depth, const uint32_t* rank, uint32_t* keys) {
+  k_mask_keys<<<blocks_for(m_max, 256, 152 * 8), 256, 0, s>>>(cells, ids, m_ptr, S, d, B, depth,
+                                                               rank, keys);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
+static inline unsigned blocks_for(uint64_t items, int threads, int cap) {
+  uint64_t b = (items + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > (uint64_t)cap) b = cap;
+  return (unsigned)b;
+}
+
+int launch_partition_skyline(cudaStream_t s, int d, int depth,
+                             const LevelTables& T, const PartitionSkylineArgs& a,
+                             const PartScratch& ps) {
+  const uint32_t K = 1u << T.B;
+  const int na = __builtin_popcount(a.S);
+  BucketScratch bs;
+  bs.keys = ps.keys;
+  bs.counts = ps.counts;
+  bs.cursor = ps.cursor;
+  k_mask_keys<<<blocks_for(a.m_max, 256, 152 * 8), 256, 0, s>>>(
+      a.cells, a.ids, a.m_ptr, a.S, d, T.B, depth, T.rank, ps.keys);
+  SKC_LAUNCH_CHECK();
+  SKC_TRY(launch_counting_sort(s, ps.keys, a.m_ptr, a.m_max, K, bs, ps.sorted, nullptr));
+  const uint64_t pitch = (a.m_max + 127) / 128 * 128;
+  k_gather_compact<<<blocks_for(a.m_max, 256, 152 * 8), 256, 0, s>>>(
+      a.cells, a.x, a.n_pad, a.ids, ps.sorted, a.m_ptr, a.S, d, pitch, ps.ccells, ps.cx);
+  SKC_LAUNCH_CHECK();
+  k_chunk_counts<<<blocks_for(K, 256, 64), 256, 0, s>>>(ps.counts, K, ps.items);
+  SKC_LAUNCH_CHECK();
+  SKC_TRY(launch_scan_single_u32(s, ps.items, K));
+  PartKernelArgs k{ps.sorted, ps.ccells, ps.cx, pitch, ps.counts, ps.items, T.unrank,
+                   T.sub_off, T.sub_list, K, a.status};
+  const unsigned grid = (unsigned)((a.m_max + 255) / 256 + K);
+#define SKC_PART_CASE(N)                                  \
+  case N:                                                 \
+    k_skyline_part<N><<<grid, 256, 0, s>>>(k);            \
+    break;
+  switch (na) {
+    SKC_PART_CASE(1) SKC_PART_CASE(2) SKC_PART_CASE(3) SKC_PART_CASE(4)
+    SKC_PART_CASE(5) SKC_PART_CASE(6) SKC_PART_CASE(7) SKC_PART_CASE(8)
+    SKC_PART_CASE(9) SKC_PART_CASE(10) SKC_PART_CASE(11) SKC_PART_CASE(12)
+    SKC_PART_CASE(13) SKC_PART_CASE(14) SKC_PART_CASE(15) SKC_PART_CASE(16)
+    default:
+      return set_error(SKC_ERR_INVALID, "subspace with %d attributes", na);
+  }
+#undef SKC_PART_CASE
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
+}  // namespace skc

@@ -590,6 +590,12 @@ int launch_scan_u32_to_u64(cudaStream_t s, const uint32_t* in, uint64_t len,
   return SKC_OK;
 }
 
+int launch_scan_single_u32(cudaStream_t s, uint32_t* a, uint32_t len) {
+  k_scan_single<uint32_t><<<1, 1024, 0, s>>>(a, len);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
 uint64_t scan_bsum_entries(uint64_t len) {
   return (len + kScanBlock - 1) / kScanBlock + 1;
 }
