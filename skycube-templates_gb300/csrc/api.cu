@@ -116,32 +116,6 @@ struct Arena {
 
 static inline uint64_t round_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
 
-static uint32_t bucket_count(uint64_t m) {
-  uint64_t k = m / 4;
-  if (k < 64) k = 64;
-  if (k > 65536) k = 65536;
-  return (uint32_t)k;
-}
-
-// Lattice-level rank of every mask: popcount ascending, then value.
-static int rank_table(skc_context* ctx, int d, const uint32_t** out) {
-  if (!ctx->d_rank_tables[d]) {
-    const uint32_t ns = 1u << d;
-    std::vector<uint32_t> order(ns), rank(ns);
-    for (uint32_t i = 0; i < ns; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [](uint32_t a, uint32_t b) {
-      return __builtin_popcount(a) < __builtin_popcount(b);
-    });
-    for (uint32_t i = 0; i < ns; ++i) rank[order[i]] = i;
-    uint32_t* p = nullptr;
-    SKC_CUDA(cudaMalloc(&p, ns * sizeof(uint32_t)));
-    SKC_CUDA(cudaMemcpy(p, rank.data(), ns * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    ctx->d_rank_tables[d] = p;
-  }
-  *out = ctx->d_rank_tables[d];
-  return SKC_OK;
-}
-
 // Partition tables over B-bit masks, built once per context (partition.cu):
 // one device buffer [rank | unrank | sub_off | sub_list].
 static int level_tables(skc_context* ctx, int B, LevelTables* out) {
@@ -603,8 +577,6 @@ int skc_context_destroy(skc_context* ctx) {
   for (skc_dataset* ds : std::vector<skc_dataset*>(ctx->datasets.begin(), ctx->datasets.end()))
     release_dataset_memory(ds);
   cudaStreamSynchronize(ctx->stream);
-  for (auto* p : ctx->d_rank_tables)
-    if (p) cudaFree(p);
   for (auto* p : ctx->d_level_tables)
     if (p) cudaFree(p);
   cudaEventDestroy(ctx->ev_start);

@@ -89,7 +89,6 @@ struct skc_context {
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
   float last_ms = 0.f;
   cudaMemPool_t pool = nullptr;
-  uint32_t* d_rank_tables[17] = {};  // level-order rank of every median mask, per d
   uint32_t* d_level_tables[11] = {};  // partition tables per B (see partition.cu)
   // Live objects created from this context; destroying the context frees
   // their device memory and detaches them (ctx = nullptr).

@@ -44,9 +44,6 @@ int launch_gather_soa(cudaStream_t s, const float* x, uint64_t n_pad, int d,
                       uint64_t out_pad, float* out);
 int launch_gather_u4(cudaStream_t s, const uint4* in, const uint32_t* perm,
                      const uint32_t* m_ptr, uint64_t m_max, uint4* out);
-int launch_level_keys(cudaStream_t s, const uint4* cells, const uint32_t* m_ptr,
-                      uint64_t m_max, int d, int depth, const uint32_t* rank,
-                      uint32_t* keys);
 int launch_block_min(cudaStream_t s, const uint4* cells, const uint32_t* m_ptr,
                      uint64_t m_max, uint4* bmin);
 int launch_csr_gather(cudaStream_t s, const uint32_t* const* srcs,

@@ -156,118 +156,142 @@ __global__ void __launch_bounds__(256) k_bitmaps(
 
     uint32_t next_blk = 0;  // blocks below this one were already visited
     uint32_t lastE = 0xffffffffu, lastQ = 0;  // last tie update applied
-    for (uint32_t b = 0; b < K; ++b) {
-      const uint32_t qbeg = boff[b], qend = boff[b + 1];
-      if (qbeg == qend) continue;
-      // Attributes where every q of the partition is above the median and p
-      // is not: no q of it is <= p there. If the rest is already strict,
-      // the whole partition adds nothing.
-      const uint32_t X = unrank[b] & ~pmask;
-      if (in_strict((NSUB - 1) & ~X)) continue;
-
-      // A block shared with the previous partition is visited once; its q's
-      // from a skipped partition are tested too (any q's update is valid).
-      const uint32_t blk_end = (qend + 31) / 32;
-      uint32_t blk = max(qbeg / 32, next_blk);
-      next_blk = blk_end;
-      for (; blk < blk_end; ++blk) {
-        const uint4 bm = bmin[blk];
-        uint32_t Ub = 0;
+    // Partitions are tested 32 at a time (lane t tests partition b0 + t):
+    // a partition is skipped when the attributes its points may win on
+    // (all but those where the partition is above the median and p is not)
+    // already form a strictly dominated subspace.
+    for (uint32_t b0 = 0; b0 < K; b0 += 32) {
+      const uint32_t bl = b0 + lane;
+      uint32_t qbeg_l = 0, qend_l = 0, Sb = 0;
+      if (bl < K) {
+        qbeg_l = boff[bl];
+        qend_l = boff[bl + 1];
+        Sb = (NSUB - 1) & ~(unrank[bl] & ~pmask);
+      }
+      // in_strict shuffles across the warp: every lane must evaluate it.
+      const bool sb_strict = in_strict(Sb);
+      const bool part_skip = (qbeg_l == qend_l) || sb_strict;
+      uint32_t parts = __ballot_sync(kFull, !part_skip);
+      while (parts) {
+        const int ps = __ffs(parts) - 1;
+        parts &= parts - 1;
+        const uint32_t qbeg = __shfl_sync(kFull, qbeg_l, ps);
+        const uint32_t qend = __shfl_sync(kFull, qend_l, ps);
+        // A block shared with the previous partition is visited once; its
+        // q's from a skipped partition are tested too (any q's update is
+        // valid).
+        const uint32_t blk_end = (qend + 31) / 32;
+        const uint32_t blk_first = max(qbeg / 32, next_blk);
+        next_blk = max(next_blk, blk_end);
+        // Blocks are tested 32 at a time against their byte-wise minimum
+        // cells, then the surviving blocks are walked one by one.
+        for (uint32_t k0 = blk_first; k0 < blk_end; k0 += 32) {
+          const uint32_t kb = k0 + lane;
+          uint32_t Ub = 0;
+          if (kb < blk_end) {
+            const uint4 bm = bmin[kb];
 #pragma unroll
-        for (int w = 0; w < NW; ++w)
-          Ub |= pack_guards(ge_bytes(pH[w], word_of(bm, w))) << (4 * w);
-        Ub &= NSUB - 1;
-        if (in_strict(Ub)) continue;  // uniform: the whole block adds nothing
-
-        const uint32_t qi = blk * 32 + lane;
-        const bool valid = qi < m;
-        uint4 q4 = make_uint4(0, 0, 0, 0);
-        if (valid) q4 = qcells[qi];
-        uint32_t U = 0;
-#pragma unroll
-        for (int w = 0; w < NW; ++w)
-          U |= pack_guards(ge_bytes(pH[w], word_of(q4, w))) << (4 * w);
-        U = valid ? (U & (NSUB - 1)) : 0u;
-        const bool hit = in_strict(U);
-        if (__all_sync(kFull, hit)) continue;
-
-        uint32_t le = 0, lt = 0;
-        if (!hit) {
-          uint32_t G = 0;  // cell(q) >= cell(p)
-#pragma unroll
-          for (int w = 0; w < NW; ++w)
-            G |= pack_guards(ge_bytes(word_of(q4, w) | kGuard, pc[w])) << (4 * w);
-          G &= NSUB - 1;
-          const uint32_t Y = U & ~G;  // certainly q < p
-          const uint32_t Z = U & G;   // equal cells: compare the floats
-          le = Y;
-          lt = Y;
-          if (Z) {
-#pragma unroll
-            for (int k = 0; k < D; ++k) {
-              if (Z & (1u << k)) {
-                const float a = qx[(uint64_t)k * p_pad + qi];
-                if (a <= pv[k]) le |= 1u << k;
-                if (a < pv[k]) lt |= 1u << k;
-              }
-            }
+            for (int w = 0; w < NW; ++w)
+              Ub |= pack_guards(ge_bytes(pH[w], word_of(bm, w))) << (4 * w);
+            Ub &= NSUB - 1;
           }
-        }
-        const bool t_lt = in_strict(lt);
-        const bool t_le = in_strict(le);
-        const bool novel = !hit && (!t_lt || (le != lt && !t_le));
-        uint32_t todo = __ballot_sync(kFull, novel);
-        while (todo) {
-          const int src = __ffs(todo) - 1;
-          todo &= todo - 1;
-          const uint32_t L = __shfl_sync(kFull, lt, src);
-          const uint32_t E = __shfl_sync(kFull, le, src);
-          // An earlier update may already cover this one.
-          const bool l_done = in_strict(L);
-          const uint32_t Q = E & ~L;  // attributes with exact ties
-          const bool e_done = (E == L) || in_strict(E) || (E == lastE && Q == lastQ);
-          if (l_done && e_done) continue;
-          if (E != L) {
-            lastE = E;
-            lastQ = Q;
-          }
-          if (REG) {
-            if (!l_done && (wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
-            if (!e_done && (wi & ~(E >> 5)) == 0) {
-              uint32_t mk = c_submask[E & 31];
-              if ((wi & ~(Q >> 5)) == 0) mk &= ~c_submask[Q & 31];
-              tie |= mk;
-            }
-          } else {
-            // Only the words under L (resp. E): the subsets of L >> 5. Lane
-            // j takes the j-th subset of the lowest five bits of L >> 5 and
-            // walks all subsets of the remaining bits.
-            if (!l_done) {
-              const uint32_t sl = c_submask[L & 31];
-              uint32_t base, rest;
-              if (split_words(L >> 5, lane, &base, &rest)) {
-                uint32_t sub = 0;
-                do {
-                  sat_s[base | sub] |= sl;
-                  sub = (sub - rest) & rest;
-                } while (sub);
+          const bool ub_strict = in_strict(Ub);  // every lane (shuffle)
+          const bool blk_skip = (kb >= blk_end) || ub_strict;
+          uint32_t blocks = __ballot_sync(kFull, !blk_skip);
+          while (blocks) {
+            const int bs = __ffs(blocks) - 1;
+            blocks &= blocks - 1;
+            const uint32_t qi = (k0 + bs) * 32 + lane;
+            const bool valid = qi < m;
+            uint4 q4 = make_uint4(0, 0, 0, 0);
+            if (valid) q4 = qcells[qi];
+            uint32_t U = 0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w)
+              U |= pack_guards(ge_bytes(pH[w], word_of(q4, w))) << (4 * w);
+            U = valid ? (U & (NSUB - 1)) : 0u;
+            const bool hit = in_strict(U);
+            if (__all_sync(kFull, hit)) continue;
+
+            uint32_t le = 0, lt = 0;
+            if (!hit) {
+              uint32_t G = 0;  // cell(q) >= cell(p)
+#pragma unroll
+              for (int w = 0; w < NW; ++w)
+                G |= pack_guards(ge_bytes(word_of(q4, w) | kGuard, pc[w])) << (4 * w);
+              G &= NSUB - 1;
+              const uint32_t Y = U & ~G;  // certainly q < p
+              const uint32_t Z = U & G;   // equal cells: compare the floats
+              le = Y;
+              lt = Y;
+              if (Z) {
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                  if (Z & (1u << k)) {
+                    const float a = qx[(uint64_t)k * p_pad + qi];
+                    if (a <= pv[k]) le |= 1u << k;
+                    if (a < pv[k]) lt |= 1u << k;
+                  }
+                }
               }
             }
-            if (!e_done) {
-              const uint32_t se = c_submask[E & 31];
-              const uint32_t sq = c_submask[Q & 31];
-              const uint32_t qh = Q >> 5;
-              uint32_t base, rest;
-              if (split_words(E >> 5, lane, &base, &rest)) {
-                uint32_t sub = 0;
-                do {
-                  const uint32_t w = base | sub;
-                  tie_s[w] |= ((w & ~qh) == 0) ? (se & ~sq) : se;
-                  sub = (sub - rest) & rest;
-                } while (sub);
+            const bool t_lt = in_strict(lt);
+            const bool t_le = in_strict(le);
+            const bool novel = !hit && (!t_lt || (le != lt && !t_le));
+            uint32_t todo = __ballot_sync(kFull, novel);
+            while (todo) {
+              const int src = __ffs(todo) - 1;
+              todo &= todo - 1;
+              const uint32_t L = __shfl_sync(kFull, lt, src);
+              const uint32_t E = __shfl_sync(kFull, le, src);
+              // An earlier update may already cover this one.
+              const bool l_done = in_strict(L);
+              const uint32_t Q = E & ~L;  // attributes with exact ties
+              const bool e_done = (E == L) || in_strict(E) || (E == lastE && Q == lastQ);
+              if (l_done && e_done) continue;
+              if (E != L) {
+                lastE = E;
+                lastQ = Q;
+              }
+              if (REG) {
+                if (!l_done && (wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
+                if (!e_done && (wi & ~(E >> 5)) == 0) {
+                  uint32_t mk = c_submask[E & 31];
+                  if ((wi & ~(Q >> 5)) == 0) mk &= ~c_submask[Q & 31];
+                  tie |= mk;
+                }
+              } else {
+                // Only the words under L (resp. E): the subsets of L >> 5.
+                // Lane j takes the j-th subset of the lowest five bits of
+                // L >> 5 and walks all subsets of the remaining bits.
+                if (!l_done) {
+                  const uint32_t sl = c_submask[L & 31];
+                  uint32_t base, rest;
+                  if (split_words(L >> 5, lane, &base, &rest)) {
+                    uint32_t sub = 0;
+                    do {
+                      sat_s[base | sub] |= sl;
+                      sub = (sub - rest) & rest;
+                    } while (sub);
+                  }
+                }
+                if (!e_done) {
+                  const uint32_t se = c_submask[E & 31];
+                  const uint32_t sq = c_submask[Q & 31];
+                  const uint32_t qh = Q >> 5;
+                  uint32_t base, rest;
+                  if (split_words(E >> 5, lane, &base, &rest)) {
+                    uint32_t sub = 0;
+                    do {
+                      const uint32_t w = base | sub;
+                      tie_s[w] |= ((w & ~qh) == 0) ? (se & ~sq) : se;
+                      sub = (sub - rest) & rest;
+                    } while (sub);
+                  }
+                }
+                __syncwarp();
               }
             }
-            __syncwarp();
           }
         }
       }

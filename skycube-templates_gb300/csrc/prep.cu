@@ -399,26 +399,6 @@ __global__ void k_gather_u4(const uint4* __restrict__ in,
     out[i] = in[perm[i]];
 }
 
-// Level-order keys of the median masks: key[i] = rank[mask(cells[i])], where
-// bit k of the mask is the top cell bit of attribute k (worse than median).
-__global__ void k_level_keys(const uint4* __restrict__ cells,
-                             const uint32_t* __restrict__ m_ptr, int d, int depth,
-                             const uint32_t* __restrict__ rank,
-                             uint32_t* __restrict__ keys) {
-  const uint32_t m = *m_ptr;
-  const int sh = depth - 1;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m;
-       i += gridDim.x * blockDim.x) {
-    const uint4 c = cells[i];
-    uint32_t mask = 0;
-    for (int k = 0; k < d; ++k) {
-      const uint32_t cell = (word_of(c, k >> 2) >> (8 * (k & 3))) & 0x7fu;
-      mask |= ((cell >> sh) & 1u) << k;
-    }
-    keys[i] = rank[mask];
-  }
-}
-
 // Per block of 32 consecutive q's: byte-wise minimum of their cells. Padding
 // entries (index >= m) get cell 127 so they never lower the minimum.
 __global__ void k_block_min(const uint4* __restrict__ cells,
@@ -611,14 +591,6 @@ int launch_gather_soa(cudaStream_t s, const float* x, uint64_t n_pad, int d,
 int launch_gather_u4(cudaStream_t s, const uint4* in, const uint32_t* perm,
                      const uint32_t* m_ptr, uint64_t m_max, uint4* out) {
   k_gather_u4<<<grid_for(m_max, 256, 152 * 8), 256, 0, s>>>(in, perm, m_ptr, out);
-  SKC_LAUNCH_CHECK();
-  return SKC_OK;
-}
-
-int launch_level_keys(cudaStream_t s, const uint4* cells, const uint32_t* m_ptr,
-                      uint64_t m_max, int d, int depth, const uint32_t* rank,
-                      uint32_t* keys) {
-  k_level_keys<<<grid_for(m_max, 256, 152 * 8), 256, 0, s>>>(cells, m_ptr, d, depth, rank, keys);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }
