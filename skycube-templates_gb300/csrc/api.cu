@@ -199,6 +199,12 @@ static int run_full_space(skc_context* ctx, skc_dataset* ds, int depth,
   SKC_TRY(A.alloc(&ps.sorted, n));
   SKC_TRY(A.alloc(&ps.ccells, n));
   SKC_TRY(A.alloc(&ps.cx, (uint64_t)d * round_up(n, 128)));
+  if (n >= kConfirmedMinPoints) {
+    SKC_TRY(A.alloc(&ps.conf_cells, n));
+    SKC_TRY(A.alloc(&ps.conf_x, (uint64_t)d * round_up(n, 128)));
+    SKC_TRY(A.alloc(&ps.ccount, K));
+    SKC_TRY(A.alloc(&ps.pdone, K));
+  }
   SKC_TRY(A.alloc(&ps.counts, K + 1));
   SKC_TRY(A.alloc(&ps.cursor, K + 1));
   SKC_TRY(A.alloc(&ps.items, K + 1));
@@ -376,6 +382,12 @@ static int run_sdsc_plain(skc_context* ctx, skc_dataset* ds, int max_d,
   SKC_TRY(A.alloc(&ps.sorted, mmax));
   SKC_TRY(A.alloc(&ps.ccells, mmax));
   SKC_TRY(A.alloc(&ps.cx, (uint64_t)d * round_up(mmax, 128)));
+  if (mmax >= kConfirmedMinPoints) {
+    SKC_TRY(A.alloc(&ps.conf_cells, mmax));
+    SKC_TRY(A.alloc(&ps.conf_x, (uint64_t)d * round_up(mmax, 128)));
+    SKC_TRY(A.alloc(&ps.ccount, Kmax));
+    SKC_TRY(A.alloc(&ps.pdone, Kmax));
+  }
   SKC_TRY(A.alloc(&ps.counts, Kmax + 1));
   SKC_TRY(A.alloc(&ps.cursor, Kmax + 1));
   SKC_TRY(A.alloc(&ps.items, Kmax + 1));

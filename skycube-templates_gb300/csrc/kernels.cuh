@@ -78,6 +78,7 @@ int launch_skyline(cudaStream_t s, int d, const SkylineArgs& a);
 // value), its inverse, and for every mask the ranks of its submasks in
 // level order.
 constexpr int kMaxPartitionDims = 10;
+constexpr uint64_t kConfirmedMinPoints = 32768;
 struct LevelTables {
   int B = 0;
   const uint32_t* rank = nullptr;      // [2^B]
@@ -90,6 +91,12 @@ struct PartScratch {
   uint32_t* sorted;  // [m_max]
   uint4* ccells;     // [m_max] compact cells in partition order
   float* cx;         // [|S| * round_up(m_max, 128)] compact floats
+  // Confirmed lists (partition.cu), used for lists of at least
+  // kConfirmedMinPoints points; nullptr disables them.
+  uint4* conf_cells = nullptr;  // [m_max]
+  float* conf_x = nullptr;      // [|S| * round_up(m_max, 128)]
+  uint32_t* ccount = nullptr;   // [2^B]
+  uint32_t* pdone = nullptr;    // [2^B]
   uint32_t* counts;  // [2^B + 1] partition offsets after the sort
   uint32_t* cursor;  // [2^B + 1]
   uint32_t* items;   // [2^B + 1]

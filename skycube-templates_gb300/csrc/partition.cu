@@ -86,6 +86,13 @@ __global__ void k_gather_compact(const uint4* __restrict__ cells,
 }
 
 struct PartKernelArgs {
+  // Confirmed lists (optional, see k_skyline_part): the points of partition b
+  // that are not strictly dominated, conf_*[boff[b] + k] for k < ccount[b],
+  // complete once pdone[b] equals b's number of work items.
+  uint4* conf_cells;
+  float* conf_x;
+  uint32_t* ccount;
+  uint32_t* pdone;
   const uint32_t* sorted;   // sorted index -> list position (for the output)
   const uint4* cells;       // compact cells in sorted order
   const float* xs;          // compact floats in sorted order, pitch `pitch`
@@ -100,16 +107,26 @@ struct PartKernelArgs {
 };
 
 // NA = number of attributes of the subspace (all of them are compared).
+//
+// Confirmed lists. Work items start in lattice-level order, so the lower
+// partitions under a CTA's mask have often finished by the time it reaches
+// them. A finished partition is read through its confirmed list (its points
+// that are not strictly dominated) instead of all its points. That is exact:
+// if a strictly dominated q dominates p, the confirmed point that strictly
+// dominates q lies in a partition under p's mask as well and strictly
+// dominates p. Nothing waits: an unfinished partition is read in full. A CTA
+// publishes its confirmed points, fences, then counts itself in pdone.
 template <int NA>
 __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
   constexpr int NW = (NA + 3) / 4;
   constexpr int TQ = 256;
   __shared__ uint4 q_cells[TQ];
   __shared__ float q_x[NA][TQ];
+  __shared__ uint32_t s_conf_end;
 
   const uint32_t nitems = a.items[a.K];
   if (blockIdx.x >= nitems) return;
-  const uint32_t it = nitems - 1 - blockIdx.x;  // heaviest partitions first
+  const uint32_t it = blockIdx.x;  // lattice-level order: lower partitions first
   uint32_t lo = 0, hi = a.K;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
@@ -130,11 +147,12 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
   for (int w = 0; w < NW; ++w) pc[w] = pH[w] = 0;
 #pragma unroll
   for (int k = 0; k < NA; ++k) pv[k] = 0.f;
+  uint4 my_cells = make_uint4(0, 0, 0, 0);
   if (valid) {
-    const uint4 c = a.cells[i];
+    my_cells = a.cells[i];
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
-      pc[w] = word_of(c, w);
+      pc[w] = word_of(my_cells, w);
       pH[w] = pc[w] | kGuard;
     }
 #pragma unroll
@@ -148,17 +166,45 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
   const uint32_t s1 = a.sub_off[mb + 1];
   for (uint32_t si = a.sub_off[mb]; si < s1 && !all_done; ++si) {
     const uint32_t qb = a.sub_list[si];
-    const uint32_t qend = a.boff[qb + 1];
-    for (uint32_t base = a.boff[qb]; base < qend; base += TQ) {
+    const uint32_t qbeg = a.boff[qb];
+    uint32_t qend = a.boff[qb + 1];
+    bool conf = false;
+    if (a.conf_cells && qb != b) {
+      if (threadIdx.x == 0) {
+        uint32_t e = 0xffffffffu;
+        const uint32_t need = a.items[qb + 1] - a.items[qb];
+        if (atomicAdd(&a.pdone[qb], 0u) == need) {
+          __threadfence();
+          e = qbeg + atomicAdd(&a.ccount[qb], 0u);
+        }
+        s_conf_end = e;
+      }
+      __syncthreads();
+      if (s_conf_end != 0xffffffffu) {
+        conf = true;
+        qend = s_conf_end;
+      }
+    }
+    const uint4* qc = conf ? a.conf_cells : a.cells;
+    const float* qxs = conf ? a.conf_x : a.xs;
+    for (uint32_t base = qbeg; base < qend; base += TQ) {
       if (__syncthreads_and(done)) {
         all_done = true;
         break;
       }
       const uint32_t j = base + threadIdx.x;
       if (j < qend) {
-        q_cells[threadIdx.x] = a.cells[j];
+        // Confirmed lists are written during this launch by other SMs: read
+        // them through L2 (ld.cg), never from a possibly stale L1 line.
+        if (conf) {
+          q_cells[threadIdx.x] = __ldcg(qc + j);
 #pragma unroll
-        for (int k = 0; k < NA; ++k) q_x[k][threadIdx.x] = a.xs[(uint64_t)k * a.pitch + j];
+          for (int k = 0; k < NA; ++k) q_x[k][threadIdx.x] = __ldcg(qxs + (uint64_t)k * a.pitch + j);
+        } else {
+          q_cells[threadIdx.x] = qc[j];
+#pragma unroll
+          for (int k = 0; k < NA; ++k) q_x[k][threadIdx.x] = qxs[(uint64_t)k * a.pitch + j];
+        }
       }
       __syncthreads();
       if (!done) {
@@ -200,6 +246,17 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
     }
   }
   if (valid) a.status[a.sorted[i]] = st;
+  if (a.conf_cells) {
+    if (valid && st != 2) {
+      const uint32_t slot = a.boff[b] + atomicAdd(&a.ccount[b], 1u);
+      a.conf_cells[slot] = my_cells;
+#pragma unroll
+      for (int k = 0; k < NA; ++k) a.conf_x[(uint64_t)k * a.pitch + slot] = pv[k];
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(&a.pdone[b], 1u);
+  }
 }
 
 static inline unsigned blocks_for(uint64_t items, int threads, int cap);
@@ -240,8 +297,12 @@ int launch_partition_skyline(cudaStream_t s, int d, int depth,
   k_chunk_counts<<<blocks_for(K, 256, 64), 256, 0, s>>>(ps.counts, K, ps.items);
   SKC_LAUNCH_CHECK();
   SKC_TRY(launch_scan_single_u32(s, ps.items, K));
-  PartKernelArgs k{ps.sorted, ps.ccells, ps.cx, pitch, ps.counts, ps.items, T.unrank,
-                   T.sub_off, T.sub_list, K, a.status};
+  PartKernelArgs k{ps.conf_cells, ps.conf_x, ps.ccount, ps.pdone, ps.sorted, ps.ccells, ps.cx,
+                   pitch, ps.counts, ps.items, T.unrank, T.sub_off, T.sub_list, K, a.status};
+  if (ps.conf_cells) {
+    SKC_CUDA(cudaMemsetAsync(ps.ccount, 0, K * sizeof(uint32_t), s));
+    SKC_CUDA(cudaMemsetAsync(ps.pdone, 0, K * sizeof(uint32_t), s));
+  }
   const unsigned grid = (unsigned)((a.m_max + 255) / 256 + K);
 #define SKC_PART_CASE(N)                                  \
   case N:                                                 \
