@@ -282,8 +282,12 @@ static int run_bitmaps(skc_context* ctx, skc_dataset* ds, const skc_options& o,
   if (want_ext) SKC_TRY(A.alloc(&ext, m * W));
   SKC_TRY(A.alloc(&work, 1));
 
+  uint64_t slab_words = 0;
+  uint32_t* slab = nullptr;
+  SKC_TRY(bitmap_tie_slab_words(d, ctx->num_sms, &slab_words));
+  if (slab_words) SKC_TRY(A.alloc(&slab, slab_words));
   BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, b.counts, LT.unrank, K, LT.B, depth,
-                m_ptr, work, 0xffffffffu, dom, ext, 0};
+                m_ptr, work, 0xffffffffu, dom, ext, 0, slab};
   if (o.mode == SKC_MODE_BATCHED) {
     SKC_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), s));
     SKC_TRY(launch_bitmaps(s, d, ctx->num_sms, ba));

@@ -137,8 +137,10 @@ struct BitmapArgs {
   uint32_t* out_dom;     // [m][words] dominated bitmaps
   uint32_t* out_ext;     // [m][words] extended-skyline bitmaps, or nullptr
   int grid_blocks;       // persistent grid (0: from occupancy)
+  uint32_t* tie_slab;    // global tie maps (bitmap_tie_slab_words), or nullptr
 };
 int launch_bitmaps(cudaStream_t s, int d, int num_sms, const BitmapArgs& a);
+int bitmap_tie_slab_words(int d, int num_sms, uint64_t* words);
 
 struct CompactArgs {
   const uint32_t* bits;  // [m][words]

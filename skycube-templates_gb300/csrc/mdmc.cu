@@ -52,13 +52,17 @@ constexpr uint32_t kFull = 0xffffffffu;
 template <int D>
 struct BitState {
   static constexpr uint32_t NSUB = 1u << D;
-  static constexpr uint32_t W = NSUB >= 32 ? NSUB / 32 : 1;
-  static constexpr bool REG = (W <= 32);
+  static constexpr uint32_t W = NSUB >= 32 ? NSUB / 32 : 1;  // bitmap words
+  static constexpr bool REG = (W <= 32);   // STRICT in registers
+  static constexpr uint32_t AW = NSUB / 2;  // tie-map words (2 entries each)
+  static constexpr bool A_SMEM = (D <= 12);  // tie map in shared memory
+  // shared memory per warp, in words
+  static constexpr uint32_t SMEM_WORDS = (REG ? 0 : W) + (A_SMEM ? AW : 0);
 };
 
-// Word w of down(L) is c_submask[L & 31] when w is a subset of L >> 5.
-// pdep_bits spreads the low bits of t over the set bits of mask: the t-th
-// subset of mask in increasing order.
+// Splits the subsets of h over 32 lanes: `low` = the lowest five set bits of
+// h, `rest` = the others. Lane j < 2^popc(low) gets base = the j-th subset
+// of low and walks every subset of rest; other lanes get nothing (false).
 __device__ __forceinline__ uint32_t pdep_bits(uint32_t t, uint32_t mask) {
   uint32_t w = 0;
   while (mask) {
@@ -70,9 +74,6 @@ __device__ __forceinline__ uint32_t pdep_bits(uint32_t t, uint32_t mask) {
   return w;
 }
 
-// Splits the subsets of h over 32 lanes: `low` = the lowest five set bits of
-// h, `rest` = the others. Lane j < 2^popc(low) gets base = the j-th subset
-// of low and walks every subset of rest; other lanes get nothing (false).
 __device__ __forceinline__ bool split_words(uint32_t h, int lane, uint32_t* base,
                                             uint32_t* rest) {
   uint32_t low = 0, t = h;
@@ -87,6 +88,45 @@ __device__ __forceinline__ bool split_words(uint32_t h, int lane, uint32_t* base
   return true;
 }
 
+// Tie map. A pair whose LE differs from LT (an exact float tie on some
+// attribute) dominates p on {S subset of LE : S meets LT}. Instead of
+// applying each such set, the warp keeps A[E] = union of LT over its tie
+// pairs with LE == E (16-bit entries, two per word). At the end one
+// superset-OR pass gives T[S] = union of A[E] over E containing S, and p is
+// dominated through ties on S exactly when S meets T[S].
+template <int D>
+__device__ void tie_closure(uint32_t* A, int lane) {
+  constexpr uint32_t AW = BitState<D>::AW;
+  for (uint32_t w = lane; w < AW; w += 32) {  // attribute 0: inside a word
+    const uint32_t x = A[w];
+    A[w] = x | (x >> 16);
+  }
+  __syncwarp();
+  for (int j = 1; j < D; ++j) {  // attribute j: words w and w + 2^(j-1)
+    const uint32_t st = 1u << (j - 1);
+    for (uint32_t t = lane; t < AW / 2; t += 32) {
+      const uint32_t w = ((t >> (j - 1)) << j) | (t & (st - 1));
+      A[w] |= A[w + st];
+    }
+    __syncwarp();
+  }
+}
+
+// Word t of the tie-dominated bitmap: bit b set iff S = 32t + b meets T[S].
+template <int D>
+__device__ __forceinline__ uint32_t tie_word(const uint32_t* A, uint32_t t) {
+  constexpr uint32_t NSUB = BitState<D>::NSUB;
+  uint32_t bits = 0;
+  const uint32_t nb = NSUB < 32 ? NSUB : 32;
+  for (uint32_t b = 0; b < nb; b += 2) {
+    const uint32_t S = 32 * t + b;
+    const uint32_t x = A[S >> 1];
+    if (S & (x & 0xffffu)) bits |= 1u << b;
+    if ((S + 1) & (x >> 16)) bits |= 2u << b;
+  }
+  return bits;
+}
+
 template <int D>
 __global__ void __launch_bounds__(256) k_bitmaps(
     const uint4* __restrict__ pcells, const float* __restrict__ px,
@@ -96,18 +136,22 @@ __global__ void __launch_bounds__(256) k_bitmaps(
     uint32_t K, int B, int depth,
     const uint32_t* __restrict__ m_ptr, uint32_t* __restrict__ work,
     uint32_t p_end_cap, uint32_t* __restrict__ out_dom,
-    uint32_t* __restrict__ out_ext) {
+    uint32_t* __restrict__ out_ext, uint32_t* __restrict__ tie_slab) {
   using BS = BitState<D>;
   constexpr int NW = (D + 3) / 4;
   constexpr uint32_t NSUB = BS::NSUB;
   constexpr uint32_t W = BS::W;
   constexpr bool REG = BS::REG;
+  constexpr uint32_t AW = BS::AW;
   extern __shared__ uint32_t smem[];
 
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  uint32_t* sat_s = REG ? nullptr : smem + (size_t)wib * 2 * W;
-  uint32_t* tie_s = REG ? nullptr : sat_s + W;
+  uint32_t* wsm = smem + (size_t)wib * BS::SMEM_WORDS;
+  uint32_t* sat_s = REG ? nullptr : wsm;
+  uint32_t* A = BS::A_SMEM
+                    ? wsm + (REG ? 0 : W)
+                    : tie_slab + ((size_t)blockIdx.x * (blockDim.x / 32) + wib) * AW;
   const uint32_t m = *m_ptr;
   const uint32_t pend = min(m, p_end_cap);
   const uint32_t wi = REG ? (uint32_t)lane % W : 0;
@@ -137,16 +181,14 @@ __global__ void __launch_bounds__(256) k_bitmaps(
 
     // STRICT starts with the empty subspace so that q's worse on every
     // attribute (U == 0) test as "nothing new".
-    uint32_t sat = 0, tie = 0;
+    uint32_t sat = 0;
     if (REG) {
       sat = (wi == 0) ? 1u : 0u;
     } else {
-      for (uint32_t w = lane; w < W; w += 32) {
-        sat_s[w] = (w == 0) ? 1u : 0u;
-        tie_s[w] = 0;
-      }
+      for (uint32_t w = lane; w < W; w += 32) sat_s[w] = (w == 0) ? 1u : 0u;
       __syncwarp();
     }
+    bool touched = false;  // tie map in use for this p
     auto in_strict = [&](uint32_t S) -> bool {
       uint32_t word;
       if (REG) word = __shfl_sync(kFull, sat, S >> 5);
@@ -155,7 +197,6 @@ __global__ void __launch_bounds__(256) k_bitmaps(
     };
 
     uint32_t next_blk = 0;  // blocks below this one were already visited
-    uint32_t lastE = 0xffffffffu, lastQ = 0;  // last tie update applied
     // Partitions are tested 32 at a time (lane t tests partition b0 + t):
     // a partition is skipped when the attributes its points may win on
     // (all but those where the partition is above the median and p is not)
@@ -237,57 +278,38 @@ __global__ void __launch_bounds__(256) k_bitmaps(
             }
             const bool t_lt = in_strict(lt);
             const bool t_le = in_strict(le);
-            const bool novel = !hit && (!t_lt || (le != lt && !t_le));
-            uint32_t todo = __ballot_sync(kFull, novel);
+            // Tie pairs go to the tie map (one atomic per lane); a tie set
+            // inside STRICT changes nothing.
+            const bool tie_lane = !hit && le != lt && !t_le;
+            if (__any_sync(kFull, tie_lane)) {
+              if (!touched) {
+                for (uint32_t w = lane; w < AW; w += 32) A[w] = 0;
+                __syncwarp();
+                touched = true;
+              }
+              if (tie_lane) atomicOr(&A[le >> 1], lt << (16 * (le & 1)));
+            }
+            // Strict updates: down(LT) into STRICT, one pair at a time.
+            uint32_t todo = __ballot_sync(kFull, !hit && !t_lt);
             while (todo) {
               const int src = __ffs(todo) - 1;
               todo &= todo - 1;
               const uint32_t L = __shfl_sync(kFull, lt, src);
-              const uint32_t E = __shfl_sync(kFull, le, src);
-              // An earlier update may already cover this one.
-              const bool l_done = in_strict(L);
-              const uint32_t Q = E & ~L;  // attributes with exact ties
-              const bool e_done = (E == L) || in_strict(E) || (E == lastE && Q == lastQ);
-              if (l_done && e_done) continue;
-              if (E != L) {
-                lastE = E;
-                lastQ = Q;
-              }
+              if (in_strict(L)) continue;  // covered by an earlier update
               if (REG) {
-                if (!l_done && (wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
-                if (!e_done && (wi & ~(E >> 5)) == 0) {
-                  uint32_t mk = c_submask[E & 31];
-                  if ((wi & ~(Q >> 5)) == 0) mk &= ~c_submask[Q & 31];
-                  tie |= mk;
-                }
+                if ((wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
               } else {
-                // Only the words under L (resp. E): the subsets of L >> 5.
-                // Lane j takes the j-th subset of the lowest five bits of
-                // L >> 5 and walks all subsets of the remaining bits.
-                if (!l_done) {
-                  const uint32_t sl = c_submask[L & 31];
-                  uint32_t base, rest;
-                  if (split_words(L >> 5, lane, &base, &rest)) {
-                    uint32_t sub = 0;
-                    do {
-                      sat_s[base | sub] |= sl;
-                      sub = (sub - rest) & rest;
-                    } while (sub);
-                  }
-                }
-                if (!e_done) {
-                  const uint32_t se = c_submask[E & 31];
-                  const uint32_t sq = c_submask[Q & 31];
-                  const uint32_t qh = Q >> 5;
-                  uint32_t base, rest;
-                  if (split_words(E >> 5, lane, &base, &rest)) {
-                    uint32_t sub = 0;
-                    do {
-                      const uint32_t w = base | sub;
-                      tie_s[w] |= ((w & ~qh) == 0) ? (se & ~sq) : se;
-                      sub = (sub - rest) & rest;
-                    } while (sub);
-                  }
+                // Only the words under L: the subsets of L >> 5. Lane j
+                // takes the j-th subset of the lowest five bits of L >> 5
+                // and walks all subsets of the remaining bits.
+                const uint32_t sl = c_submask[L & 31];
+                uint32_t base, rest;
+                if (split_words(L >> 5, lane, &base, &rest)) {
+                  uint32_t sub = 0;
+                  do {
+                    sat_s[base | sub] |= sl;
+                    sub = (sub - rest) & rest;
+                  } while (sub);
                 }
                 __syncwarp();
               }
@@ -297,9 +319,15 @@ __global__ void __launch_bounds__(256) k_bitmaps(
       }
     }
 
-    // Output: dominated = STRICT | TIE, extended = TIE \ STRICT. Bit 0 (the
-    // empty subspace) is cleared.
+    // Output: dominated = STRICT | TIE, extended = TIE \ STRICT, with TIE
+    // from the closed tie map. Bit 0 (the empty subspace) is cleared.
+    if (touched) {
+      __syncwarp();
+      tie_closure<D>(A, lane);
+    }
     if (REG) {
+      uint32_t tie = 0;
+      if (touched && (uint32_t)lane < W) tie = tie_word<D>(A, lane);
       if ((uint32_t)lane < W) {
         uint32_t dom = sat | tie, ext = tie & ~sat;
         if (lane == 0) {
@@ -311,7 +339,8 @@ __global__ void __launch_bounds__(256) k_bitmaps(
       }
     } else {
       for (uint32_t w = lane; w < W; w += 32) {
-        uint32_t s_ = sat_s[w], t_ = tie_s[w];
+        const uint32_t s_ = sat_s[w];
+        const uint32_t t_ = touched ? tie_word<D>(A, w) : 0u;
         uint32_t dom = s_ | t_, ext = t_ & ~s_;
         if (w == 0) {
           dom &= ~1u;
@@ -320,51 +349,82 @@ __global__ void __launch_bounds__(256) k_bitmaps(
         out_dom[(uint64_t)p * W + w] = dom;
         if (out_ext) out_ext[(uint64_t)p * W + w] = ext;
       }
-      __syncwarp();
     }
+    __syncwarp();
   }
 }
 
 template <int D>
-static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
+static int bitmap_grid_d(int num_sms, int* grid, size_t* smem) {
   using BS = BitState<D>;
   constexpr int threads = 256;
-  const size_t smem = BS::REG ? 0 : (size_t)(threads / 32) * 2 * BS::W * sizeof(uint32_t);
-  if (smem > 48 * 1024)
-    SKC_CUDA(cudaFuncSetAttribute(k_bitmaps<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int grid = a.grid_blocks;
-  if (grid <= 0) {
-    int per_sm = 0;
-    SKC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmaps<D>, threads, smem));
-    if (per_sm < 1) per_sm = 1;
-    grid = per_sm * num_sms;
-  }
-  k_bitmaps<D><<<grid, threads, smem, s>>>(a.pcells, a.px, a.p_pad, a.qcells, a.qx,
-                                           a.bmin, a.boff, a.unrank, a.K, a.B, a.depth,
-                                           a.m_ptr, a.work, a.p_end, a.out_dom, a.out_ext);
+  *smem = (size_t)(threads / 32) * BS::SMEM_WORDS * sizeof(uint32_t);
+  if (*smem > 48 * 1024)
+    SKC_CUDA(cudaFuncSetAttribute(k_bitmaps<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem));
+  int per_sm = 0;
+  SKC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmaps<D>, threads, *smem));
+  if (per_sm < 1) per_sm = 1;
+  if (!BS::A_SMEM && per_sm > 4) per_sm = 4;  // bounds the global tie-map slab
+  *grid = per_sm * num_sms;
+  return SKC_OK;
+}
+
+template <int D>
+static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
+  int grid = 0;
+  size_t smem = 0;
+  SKC_TRY(bitmap_grid_d<D>(num_sms, &grid, &smem));
+  if (a.grid_blocks > 0 && a.grid_blocks < grid) grid = a.grid_blocks;
+  k_bitmaps<D><<<grid, 256, smem, s>>>(a.pcells, a.px, a.p_pad, a.qcells, a.qx,
+                                        a.bmin, a.boff, a.unrank, a.K, a.B, a.depth,
+                                        a.m_ptr, a.work, a.p_end, a.out_dom, a.out_ext,
+                                        a.tie_slab);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }
 
-int launch_bitmaps(cudaStream_t s, int d, int num_sms, const BitmapArgs& a) {
-  switch (d) {
-    case 2: return launch_bitmaps_d<2>(s, num_sms, a);
-    case 3: return launch_bitmaps_d<3>(s, num_sms, a);
-    case 4: return launch_bitmaps_d<4>(s, num_sms, a);
-    case 5: return launch_bitmaps_d<5>(s, num_sms, a);
-    case 6: return launch_bitmaps_d<6>(s, num_sms, a);
-    case 7: return launch_bitmaps_d<7>(s, num_sms, a);
-    case 8: return launch_bitmaps_d<8>(s, num_sms, a);
-    case 9: return launch_bitmaps_d<9>(s, num_sms, a);
-    case 10: return launch_bitmaps_d<10>(s, num_sms, a);
-    case 11: return launch_bitmaps_d<11>(s, num_sms, a);
-    case 12: return launch_bitmaps_d<12>(s, num_sms, a);
-    case 13: return launch_bitmaps_d<13>(s, num_sms, a);
-    case 14: return launch_bitmaps_d<14>(s, num_sms, a);
-    case 15: return launch_bitmaps_d<15>(s, num_sms, a);
-    case 16: return launch_bitmaps_d<16>(s, num_sms, a);
-    default: return set_error(SKC_ERR_INVALID, "unsupported d=%d", d);
+#define SKC_BITMAP_DISPATCH(fn, ...)                    \
+  switch (d) {                                          \
+    case 2: return fn<2>(__VA_ARGS__);                  \
+    case 3: return fn<3>(__VA_ARGS__);                  \
+    case 4: return fn<4>(__VA_ARGS__);                  \
+    case 5: return fn<5>(__VA_ARGS__);                  \
+    case 6: return fn<6>(__VA_ARGS__);                  \
+    case 7: return fn<7>(__VA_ARGS__);                  \
+    case 8: return fn<8>(__VA_ARGS__);                  \
+    case 9: return fn<9>(__VA_ARGS__);                  \
+    case 10: return fn<10>(__VA_ARGS__);                \
+    case 11: return fn<11>(__VA_ARGS__);                \
+    case 12: return fn<12>(__VA_ARGS__);                \
+    case 13: return fn<13>(__VA_ARGS__);                \
+    case 14: return fn<14>(__VA_ARGS__);                \
+    case 15: return fn<15>(__VA_ARGS__);                \
+    case 16: return fn<16>(__VA_ARGS__);                \
+    default: return set_error(SKC_ERR_INVALID, "unsupported d=%d", d); \
   }
+
+int launch_bitmaps(cudaStream_t s, int d, int num_sms, const BitmapArgs& a) {
+  SKC_BITMAP_DISPATCH(launch_bitmaps_d, s, num_sms, a)
+}
+
+template <int D>
+static int slab_words_d(int num_sms, uint64_t* words) {
+  using BS = BitState<D>;
+  if (BS::A_SMEM) {
+    *words = 0;
+    return SKC_OK;
+  }
+  int grid = 0;
+  size_t smem = 0;
+  SKC_TRY(bitmap_grid_d<D>(num_sms, &grid, &smem));
+  *words = (uint64_t)grid * 8 * BS::AW;
+  return SKC_OK;
+}
+
+// Words of global memory the bitmap kernel needs for its tie maps (0 when
+// they fit in shared memory).
+int bitmap_tie_slab_words(int d, int num_sms, uint64_t* words) {
+  SKC_BITMAP_DISPATCH(slab_words_d, num_sms, words)
 }
 
 // --------------------------------------------------------------------------
