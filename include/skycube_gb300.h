@@ -110,7 +110,8 @@ int skc_result_info(skc_result* res, int* d, uint64_t* n_candidates,
                     uint64_t* total_skyline_ids);
 
 /* Host view of one cuboid's skyline ids (ascending). The pointer stays valid
- * until skc_result_free. Cuboids above max_d report count 0. */
+ * until skc_result_free. Cuboids above max_d report count 0, except the full
+ * space, which is always computed (as the suite does). */
 int skc_result_cuboid(skc_result* res, uint32_t cuboid, const uint32_t** ids,
                       uint64_t* count);
 /* Host view of one cuboid's extended skyline ids (needs want_extended). */

@@ -461,7 +461,7 @@ static int run_sdsc_plain(skc_context* ctx, skc_dataset* ds, int max_d,
     const auto& cntv = pass == 0 ? nsky : next;
     const auto& srcv = pass == 0 ? sky : ext;
     for (uint32_t c = 0; c < nsub; ++c) {
-      const bool want = c >= 1 && __builtin_popcount(c) <= max_d;
+      const bool want = c >= 1 && (__builtin_popcount(c) <= max_d || c == full);
       off[c + 1] = off[c] + (want ? cntv[c] : 0);
     }
     uint64_t* d_off;

@@ -438,8 +438,10 @@ uint32_t compact_tiles(uint64_t m_max) {
   return (uint32_t)(t ? t : 1);
 }
 
+// Cuboids within max_d, plus the full space, which is always computed (the
+// suite computes it first in both algorithms).
 __device__ __forceinline__ bool cuboid_wanted(uint32_t c, uint32_t nsub, int max_d) {
-  return c >= 1 && c < nsub && __popc(c) <= max_d;
+  return c >= 1 && c < nsub && (__popc(c) <= max_d || c == nsub - 1);
 }
 
 // Bits of row r's word w that count (1 = counted).

@@ -204,10 +204,10 @@ class Result:
         return self._view(lib().skc_result_extended, cuboid)
 
     def all_cuboids(self, extended=False):
-        """{cuboid mask: ids} for every cuboid within max_d."""
+        """{cuboid mask: ids} for every cuboid within max_d and the full space."""
         out = {}
         for c in range(1, 1 << self.d):
-            if bin(c).count("1") <= self.max_d:
+            if bin(c).count("1") <= self.max_d or c == (1 << self.d) - 1:
                 out[c] = self.extended(c) if extended else self.cuboid(c)
         return out
 
