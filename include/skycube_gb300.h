@@ -80,6 +80,8 @@ typedef struct skc_options {
   int depth;       /* grid depth: 2^depth cells per attribute, 1..7; 0: auto (-d) */
   int want_extended; /* also produce per-cuboid extended skylines */
   int want_bitmaps;  /* keep per-point bitmaps for skc_result_bitmaps */
+  uint32_t subspace; /* 0: the skycube; a cuboid mask: only that cuboid's
+                        skyline and extended skyline (a skyline query) */
 } skc_options;
 
 /* Fills *opt with defaults: MDMC, BATCHED, all cuboids, auto depth. */
@@ -132,6 +134,41 @@ int skc_result_bitmaps(skc_result* res, const uint32_t** bits,
                        const uint32_t** pids, uint64_t* n_points,
                        uint32_t* words);
 int skc_result_free(skc_result* res);
+
+/* ---- Serving loop (continuous batching) ---------------------------------
+ * A server owns `slots` worker threads, each with its own CUDA stream.
+ * Submitted requests wait in FIFO order; the first one starts as soon as a
+ * slot is free and its estimated device-memory footprint fits what the
+ * requests in flight leave of `budget` (bytes; 0: 80% of the free device
+ * memory). Requests whose estimate exceeds the whole budget are rejected
+ * with SKC_ERR_REJECTED at submission. Requests that run at the same time
+ * overlap on the device. Results come back in host memory (their device
+ * views are empty). Host rows passed to skc_server_submit must stay valid
+ * until skc_server_wait returns for that ticket. A server and its requests
+ * may be used from several host threads. */
+typedef struct skc_server skc_server;
+typedef struct skc_server_timing {
+  double queued_ms;  /* submission to admission */
+  double run_ms;     /* admission to completion (upload, compute, copy out) */
+  double total_ms;   /* submission to completion: the request's latency */
+  float device_ms;   /* device time of the computation (CUDA events) */
+} skc_server_timing;
+
+int skc_server_create(skc_context* ctx, int slots, uint64_t budget,
+                      skc_server** out);
+/* Request on host rows (n x d row-major float32), uploaded by the server. */
+int skc_server_submit(skc_server* srv, const float* rows, uint64_t n, int d,
+                      const skc_options* opt, uint64_t* ticket);
+/* Request on a dataset already resident on the server's context. */
+int skc_server_submit_dataset(skc_server* srv, skc_dataset* ds,
+                              const skc_options* opt, uint64_t* ticket);
+/* Blocks until the request is done; hands its result to the caller. */
+int skc_server_wait(skc_server* srv, uint64_t ticket, skc_result** out,
+                    skc_server_timing* timing);
+int skc_server_stats(skc_server* srv, uint64_t* admitted,
+                     uint64_t* peak_in_flight, uint64_t* budget);
+/* Waits for queued and running requests, then stops the workers. */
+int skc_server_destroy(skc_server* srv);
 
 /* Milliseconds of device time of the last skc_skycube on this context,
  * measured with CUDA events on the context's stream. */

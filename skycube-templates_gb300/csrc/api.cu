@@ -28,6 +28,12 @@
 //               tombstoning_hearting_gpu (src/mdmc/MDMC.cu:752-857).
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <thread>
 #include <cstdarg>
 #include <cstdlib>
 #include <cstdio>
@@ -57,32 +63,44 @@ void clear_error() { g_err.clear(); }
 static std::atomic<uint64_t> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
-// Per-phase device timing: CUDA events on the context's stream, kept on the
-// context (skc_last_phase) and printed to stderr when SKC_TRACE=1.
+// Execution state of one pipeline run: the stream it is issued on and the
+// per-phase device times (CUDA events on that stream). skc_skycube runs on
+// the context's stream; each serving slot has its own.
+struct Exec {
+  skc_context* ctx = nullptr;
+  cudaStream_t stream = nullptr;
+  std::vector<std::pair<std::string, float>> phases;
+  float ms = 0.f;
+};
+
+// Records phase marks on the Exec's stream; fills Exec::phases when it goes
+// out of scope and prints them to stderr when SKC_TRACE=1.
 struct Tracer {
-  skc_context* ctx;
+  Exec& E;
   bool print;
   std::vector<std::pair<const char*, cudaEvent_t>> marks;
-  explicit Tracer(skc_context* c) : ctx(c) {
-    const char* e = getenv("SKC_TRACE");
-    print = e && *e && *e != '0';
+  explicit Tracer(Exec& e) : E(e) {
+    const char* v = getenv("SKC_TRACE");
+    print = v && *v && *v != '0';
     mark("start");
   }
   void mark(const char* name) {
     cudaEvent_t ev;
     if (cudaEventCreate(&ev) != cudaSuccess) return;
-    cudaEventRecord(ev, ctx->stream);
+    cudaEventRecord(ev, E.stream);
     marks.push_back({name, ev});
   }
   ~Tracer() {
-    ctx->phases.clear();
-    if (!marks.empty() && cudaEventSynchronize(marks.back().second) == cudaSuccess) {
+    E.phases.clear();
+    E.ms = 0.f;
+    if (marks.size() > 1 && cudaEventSynchronize(marks.back().second) == cudaSuccess) {
       for (size_t i = 1; i < marks.size(); ++i) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, marks[i - 1].second, marks[i].second);
-        ctx->phases.push_back({marks[i].first, ms});
+        E.phases.push_back({marks[i].first, ms});
         if (print) fprintf(stderr, "[skc] %-24s %9.3f ms\n", marks[i].first, ms);
       }
+      cudaEventElapsedTime(&E.ms, marks.front().second, marks.back().second);
     }
     for (auto& m : marks) cudaEventDestroy(m.second);
   }
@@ -120,6 +138,7 @@ static inline uint64_t round_up(uint64_t v, uint64_t a) { return (v + a - 1) / a
 // one device buffer [rank | unrank | sub_off | sub_list].
 static int level_tables(skc_context* ctx, int B, LevelTables* out) {
   const uint32_t ns = 1u << B;
+  std::lock_guard<std::mutex> lock(ctx->mu);
   if (!ctx->d_level_tables[B]) {
     std::vector<uint32_t> order(ns), rank(ns);
     for (uint32_t i = 0; i < ns; ++i) order[i] = i;
@@ -176,9 +195,10 @@ struct FullSpace {
   uint32_t h_counts[3] = {0, 0, 0};
 };
 
-static int run_full_space(skc_context* ctx, skc_dataset* ds, int depth,
-                          Arena& A, FullSpace& F, Tracer& T) {
-  cudaStream_t s = ctx->stream;
+static int run_full_space(Exec& E, skc_dataset* ds, int depth, Arena& A,
+                          FullSpace& F, Tracer& T) {
+  skc_context* ctx = E.ctx;
+  cudaStream_t s = E.stream;
   const uint64_t n = ds->n;
   const int d = ds->d;
   const uint32_t full = (1u << d) - 1;
@@ -233,10 +253,11 @@ static int run_full_space(skc_context* ctx, skc_dataset* ds, int depth,
 }
 
 // Bitmaps of every candidate, then CSR compaction (BATCHED and PLAIN/MDMC).
-static int run_bitmaps(skc_context* ctx, skc_dataset* ds, const skc_options& o,
+static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
                        int depth, int max_d, Arena& A, FullSpace& F,
                        skc_result* R, Tracer& T) {
-  cudaStream_t s = ctx->stream;
+  skc_context* ctx = E.ctx;
+  cudaStream_t s = E.stream;
   const int d = ds->d;
   const uint32_t nsub = 1u << d;
   const uint32_t W = nsub >= 32 ? nsub / 32 : 1;
@@ -366,10 +387,11 @@ static int run_bitmaps(skc_context* ctx, skc_dataset* ds, const skc_options& o,
 }
 
 // The suite's per-cuboid schedule (PLAIN/SDSC).
-static int run_sdsc_plain(skc_context* ctx, skc_dataset* ds, int max_d,
+static int run_sdsc_plain(Exec& E, skc_dataset* ds, int max_d,
                           int depth_of_call, Arena& A, FullSpace& F,
                           skc_result* R, Tracer& T) {
-  cudaStream_t s = ctx->stream;
+  skc_context* ctx = E.ctx;
+  cudaStream_t s = E.stream;
   const int d = ds->d;
   const uint32_t nsub = 1u << d, full = nsub - 1;
   std::vector<uint32_t*> sky(nsub, nullptr), ext(nsub, nullptr);
@@ -506,7 +528,7 @@ using namespace skc;
 // struct stays valid until the caller frees it.
 static void release_result_memory(skc_result* r) {
   if (!r->ctx) return;
-  cudaStream_t s = r->ctx->stream;
+  cudaStream_t s = r->stream ? r->stream : r->ctx->stream;
   for (void* p : {(void*)r->d_off, (void*)r->d_ids, (void*)r->d_eoff, (void*)r->d_eids,
                   (void*)r->d_bits, (void*)r->d_cand})
     if (p) cudaFreeAsync(p, s);
@@ -516,15 +538,21 @@ static void release_result_memory(skc_result* r) {
   r->d_eids = nullptr;
   r->d_bits = nullptr;
   r->d_cand = nullptr;
-  r->ctx->results.erase(r);
+  {
+    std::lock_guard<std::mutex> lock(r->ctx->mu);
+    r->ctx->results.erase(r);
+  }
   r->ctx = nullptr;
 }
 
 static void release_dataset_memory(skc_dataset* ds) {
   if (!ds->ctx) return;
-  if (ds->x) cudaFreeAsync(ds->x, ds->ctx->stream);
+  if (ds->x) cudaFreeAsync(ds->x, ds->stream ? ds->stream : ds->ctx->stream);
   ds->x = nullptr;
-  ds->ctx->datasets.erase(ds);
+  {
+    std::lock_guard<std::mutex> lock(ds->ctx->mu);
+    ds->ctx->datasets.erase(ds);
+  }
   ds->ctx = nullptr;
 }
 
@@ -554,6 +582,7 @@ void skc_options_init(skc_options* o) {
   o->depth = 0;
   o->want_extended = 0;
   o->want_bitmaps = 0;
+  o->subspace = 0;
 }
 
 int skc_context_create(int device, skc_context** out) {
@@ -602,19 +631,28 @@ int skc_context_destroy(skc_context* ctx) {
   return SKC_OK;
 }
 
+static int upload_on(skc_context* ctx, cudaStream_t s, const float* rows, uint64_t n,
+                     int d, bool from_host, skc_dataset** out);
+
 static int upload_common(skc_context* ctx, const float* rows, uint64_t n, int d,
                          bool from_host, skc_dataset** out) {
   clear_error();
   if (!ctx || !rows || !out) return set_error(SKC_ERR_INVALID, "NULL argument");
+  return upload_on(ctx, ctx->stream, rows, n, d, from_host, out);
+}
+
+// Uploads on stream s (the context's stream, or a serving slot's).
+static int upload_on(skc_context* ctx, cudaStream_t s, const float* rows, uint64_t n,
+                     int d, bool from_host, skc_dataset** out) {
   *out = nullptr;
   if (d < SKC_MIN_DIMS || d > SKC_MAX_DIMS)
     return set_error(SKC_ERR_INVALID, "d=%d outside [%d,%d]", d, SKC_MIN_DIMS, SKC_MAX_DIMS);
   if (n == 0) return set_error(SKC_ERR_INVALID, "empty dataset (n=0)");
   if (n > 0xffffff00ull) return set_error(SKC_ERR_UNSUPPORTED, "n=%llu exceeds 32-bit point ids", (unsigned long long)n);
   SKC_CUDA(cudaSetDevice(ctx->device));
-  cudaStream_t s = ctx->stream;
   auto* ds = new skc_dataset;
   ds->ctx = ctx;
+  ds->stream = s;
   ds->n = n;
   ds->d = d;
   ds->n_pad = round_up(n, 128);
@@ -646,7 +684,10 @@ static int upload_common(skc_context* ctx, const float* rows, uint64_t n, int d,
     delete ds;
     return st;
   }
-  ctx->datasets.insert(ds);
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->datasets.insert(ds);
+  }
   *out = ds;
   return SKC_OK;
 }
@@ -665,11 +706,155 @@ int skc_dataset_free(skc_dataset* ds) {
   if (!ds) return SKC_OK;
   if (ds->ctx) {
     skc_context* ctx = ds->ctx;
+    cudaStream_t s = ds->stream ? ds->stream : ctx->stream;
     cudaSetDevice(ctx->device);
     release_dataset_memory(ds);
-    cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(s);
   }
   delete ds;
+  return SKC_OK;
+}
+
+// Validates options against a dataset; fills *o with defaults where unset.
+static int check_options(skc_dataset* ds, const skc_options* opt, skc_options* o) {
+  skc_options_init(o);
+  if (opt) *o = *opt;
+  if (o->algo != SKC_ALGO_MDMC && o->algo != SKC_ALGO_SDSC)
+    return set_error(SKC_ERR_INVALID, "unknown algorithm %d", o->algo);
+  if (o->mode != SKC_MODE_PLAIN && o->mode != SKC_MODE_BATCHED)
+    return set_error(SKC_ERR_INVALID, "unknown mode %d", o->mode);
+  if (o->depth < 0 || o->depth > kMaxDepth)
+    return set_error(SKC_ERR_INVALID, "depth %d outside [1,%d] (0 = auto)", o->depth, kMaxDepth);
+  if (o->subspace >= (1u << ds->d))
+    return set_error(SKC_ERR_INVALID, "subspace 0x%x has attributes beyond d=%d", o->subspace, ds->d);
+  return SKC_OK;
+}
+
+// Skyline query: one cuboid S only. The full-space skyline plus extended
+// skyline holds every point that can be in S's skyline or extended skyline
+// (a point strictly dominated in the full space is strictly dominated in S),
+// so S is computed over those candidates.
+static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, int depth,
+                             Arena& A, FullSpace& F, skc_result* R, Tracer& T) {
+  cudaStream_t s = E.stream;
+  const int d = ds->d;
+  const uint32_t nsub = 1u << d, full = nsub - 1;
+  uint32_t *sky = F.sky, *ext = F.ext;
+  uint64_t nsky = F.h_counts[0], next = F.h_counts[1];
+  if (S != full) {
+    const uint64_t m = F.h_counts[2];
+    LevelTables LT;
+    SKC_TRY(level_tables(E.ctx, partition_dims(S), &LT));
+    const uint32_t K = 1u << LT.B;
+    PartScratch ps;
+    SKC_TRY(A.alloc(&ps.keys, m));
+    SKC_TRY(A.alloc(&ps.sorted, m));
+    SKC_TRY(A.alloc(&ps.ccells, m));
+    SKC_TRY(A.alloc(&ps.cx, (uint64_t)d * round_up(m, 128)));
+    SKC_TRY(A.alloc(&ps.counts, K + 1));
+    SKC_TRY(A.alloc(&ps.cursor, K + 1));
+    SKC_TRY(A.alloc(&ps.items, K + 1));
+    if (m >= kConfirmedMinPoints) {
+      SKC_TRY(A.alloc(&ps.conf_cells, m));
+      SKC_TRY(A.alloc(&ps.conf_x, (uint64_t)d * round_up(m, 128)));
+      SKC_TRY(A.alloc(&ps.ccount, K));
+      SKC_TRY(A.alloc(&ps.pdone, K));
+    }
+    uint8_t* status;
+    uint32_t *blk0, *blk1, *cnt;
+    SKC_TRY(A.alloc(&status, m));
+    const uint64_t nblk = (m + 1023) / 1024 + 1;
+    SKC_TRY(A.alloc(&blk0, nblk));
+    SKC_TRY(A.alloc(&blk1, nblk));
+    SKC_TRY(A.alloc(&cnt, 2));
+    SKC_TRY(A.alloc(&sky, m));
+    SKC_TRY(A.alloc(&ext, m));
+    uint32_t* m_ptr = F.counts + 2;
+    PartitionSkylineArgs pa{F.cand, F.cells, ds->x, ds->n_pad, m_ptr, m, S, status};
+    SKC_TRY(launch_partition_skyline(s, d, depth, LT, pa, ps));
+    SKC_TRY(launch_status_compact(s, status, F.cand, m_ptr, m, 0, blk0, blk1, sky, ext, cnt, cnt + 1));
+    uint32_t h[2] = {0, 0};
+    SKC_CUDA(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SKC_CUDA(cudaStreamSynchronize(s));
+    nsky = h[0];
+    next = h[1];
+    T.mark("subspace skyline");
+  }
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<uint64_t> off(nsub + 1, 0);
+    const uint64_t cntc = pass == 0 ? nsky : next;
+    for (uint32_t c = 0; c < nsub; ++c) off[c + 1] = off[c] + (c == S ? cntc : 0);
+    uint64_t* d_off;
+    SKC_TRY(A.alloc(&d_off, nsub + 1));
+    SKC_CUDA(cudaMemcpyAsync(d_off, off.data(), (nsub + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    SKC_CUDA(cudaStreamSynchronize(s));  // `off` is a host temporary
+    uint32_t* ids = pass == 0 ? sky : ext;
+    A.release(d_off);
+    A.release(ids);
+    if (pass == 0) {
+      R->d_off = d_off;
+      R->d_ids = ids;
+      R->total_ids = cntc;
+    } else {
+      R->d_eoff = d_off;
+      R->d_eids = ids;
+      R->total_ext = cntc;
+    }
+  }
+  return SKC_OK;
+}
+
+// Runs one skycube (or skyline query) on E's stream; on success *out is a
+// new result registered with the context.
+static int skycube_exec(Exec& E, skc_dataset* ds, const skc_options* opt, skc_result** out) {
+  skc_context* ctx = E.ctx;
+  skc_options o;
+  SKC_TRY(check_options(ds, opt, &o));
+  const int d = ds->d;
+  const int max_d = (o.max_d <= 0 || o.max_d > d) ? d : o.max_d;
+  const int depth = o.depth ? o.depth : auto_depth(ds->n, d);
+  SKC_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = E.stream;
+
+  auto* R = new skc_result;
+  R->ctx = ctx;
+  R->stream = s;
+  R->d = d;
+  R->max_d = o.subspace ? __builtin_popcount(o.subspace) : max_d;
+  R->algo = o.algo;
+  int st = SKC_OK;
+  {
+    Arena A(s);
+    FullSpace F;
+    Tracer T(E);
+    st = run_full_space(E, ds, depth, A, F, T);
+    if (st == SKC_OK) {
+      R->n_cand = F.h_counts[2];
+      if (o.subspace) {
+        st = run_single_cuboid(E, ds, o.subspace, depth, A, F, R, T);
+      } else if (o.algo == SKC_ALGO_SDSC && o.mode == SKC_MODE_PLAIN) {
+        st = run_sdsc_plain(E, ds, max_d, depth, A, F, R, T);
+      } else {
+        st = run_bitmaps(E, ds, o, depth, max_d, A, F, R, T);
+      }
+    }
+    T.mark("end");
+  }
+  if (st == SKC_OK) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = set_error(SKC_ERR_CUDA, "skycube failed: %s", cudaGetErrorString(e));
+  }
+  if (st != SKC_OK) {
+    std::string msg = g_err;
+    skc_result_free(R);
+    g_err = msg;
+    return st;
+  }
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->results.insert(R);
+  }
+  *out = R;
   return SKC_OK;
 }
 
@@ -678,61 +863,13 @@ int skc_skycube(skc_context* ctx, skc_dataset* ds, const skc_options* opt, skc_r
   if (!ctx || !ds || !out) return set_error(SKC_ERR_INVALID, "NULL argument");
   *out = nullptr;
   if (ds->ctx != ctx) return set_error(SKC_ERR_INVALID, "dataset belongs to another (or a destroyed) context");
-  skc_options o;
-  skc_options_init(&o);
-  if (opt) o = *opt;
-  if (o.algo != SKC_ALGO_MDMC && o.algo != SKC_ALGO_SDSC)
-    return set_error(SKC_ERR_INVALID, "unknown algorithm %d", o.algo);
-  if (o.mode != SKC_MODE_PLAIN && o.mode != SKC_MODE_BATCHED)
-    return set_error(SKC_ERR_INVALID, "unknown mode %d", o.mode);
-  if (o.depth < 0 || o.depth > kMaxDepth)
-    return set_error(SKC_ERR_INVALID, "depth %d outside [1,%d] (0 = auto)", o.depth, kMaxDepth);
-  const int d = ds->d;
-  const int max_d = (o.max_d <= 0 || o.max_d > d) ? d : o.max_d;
-  const int depth = o.depth ? o.depth : auto_depth(ds->n, d);
-  SKC_CUDA(cudaSetDevice(ctx->device));
-  cudaStream_t s = ctx->stream;
-
-  auto* R = new skc_result;
-  R->ctx = ctx;
-  R->d = d;
-  R->max_d = max_d;
-  R->algo = o.algo;
-  int st = SKC_OK;
-  {
-    Arena A(s);
-    FullSpace F;
-    cudaEventRecord(ctx->ev_start, s);
-    Tracer T(ctx);
-    st = run_full_space(ctx, ds, depth, A, F, T);
-    if (st == SKC_OK) {
-      R->n_cand = F.h_counts[2];
-      if (o.algo == SKC_ALGO_SDSC && o.mode == SKC_MODE_PLAIN) {
-        A.release(F.sky);
-        A.release(F.ext);
-        st = run_sdsc_plain(ctx, ds, max_d, depth, A, F, R, T);
-        cudaFreeAsync(F.sky, s);
-        cudaFreeAsync(F.ext, s);
-      } else {
-        st = run_bitmaps(ctx, ds, o, depth, max_d, A, F, R, T);
-      }
-    }
-    cudaEventRecord(ctx->ev_stop, s);
-  }
-  if (st == SKC_OK) {
-    cudaError_t e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) st = set_error(SKC_ERR_CUDA, "skycube failed: %s", cudaGetErrorString(e));
-  }
-  if (st == SKC_OK) cudaEventElapsedTime(&ctx->last_ms, ctx->ev_start, ctx->ev_stop);
-  if (st != SKC_OK) {
-    std::string msg = g_err;
-    skc_result_free(R);
-    g_err = msg;
-    return st;
-  }
-  ctx->results.insert(R);
-  *out = R;
-  return SKC_OK;
+  Exec E;
+  E.ctx = ctx;
+  E.stream = ctx->stream;
+  const int st = skycube_exec(E, ds, opt, out);
+  ctx->phases = E.phases;
+  ctx->last_ms = E.ms;
+  return st;
 }
 
 int skc_result_info(skc_result* r, int* d, uint64_t* n_cand, uint64_t* total) {
@@ -754,7 +891,7 @@ static int download_csr(skc_result* r, bool ext) {
   auto& off = ext ? r->h_eoff : r->h_off;
   auto& ids = ext ? r->h_eids : r->h_ids;
   const uint32_t nsub = 1u << r->d;
-  cudaStream_t s = r->ctx->stream;
+  cudaStream_t s = r->stream;
   SKC_CUDA(cudaSetDevice(r->ctx->device));
   off.resize(nsub + 1);
   SKC_CUDA(cudaMemcpyAsync(off.data(), d_off, (nsub + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
@@ -809,7 +946,7 @@ int skc_result_bitmaps(skc_result* r, const uint32_t** bits, const uint32_t** pi
   if (!r->bits_downloaded && !r->d_bits) return set_error(SKC_ERR_INVALID, "bitmaps were not requested (want_bitmaps)");
   if (!r->bits_downloaded) {
     SKC_CUDA(cudaSetDevice(r->ctx->device));
-    cudaStream_t s = r->ctx->stream;
+    cudaStream_t s = r->stream;
     r->h_bits.resize(r->n_cand * r->words);
     r->h_cand.resize(r->n_cand);
     if (r->n_cand) {
@@ -830,9 +967,10 @@ int skc_result_free(skc_result* r) {
   if (!r) return SKC_OK;
   if (r->ctx) {
     skc_context* ctx = r->ctx;
+    cudaStream_t s = r->stream ? r->stream : ctx->stream;
     cudaSetDevice(ctx->device);
     release_result_memory(r);
-    cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(s);
   }
   delete r;
   return SKC_OK;
@@ -842,6 +980,292 @@ int skc_last_device_ms(skc_context* ctx, float* ms) {
   clear_error();
   if (!ctx || !ms) return set_error(SKC_ERR_INVALID, "NULL argument");
   *ms = ctx->last_ms;
+  return SKC_OK;
+}
+
+}  // extern "C"
+
+// ==========================================================================
+// Serving loop (continuous batching). Requests wait in a FIFO queue; each of
+// `slots` workers owns a CUDA stream and host thread. The head request is
+// admitted as soon as a worker is free and its estimated device-memory
+// footprint fits the budget left by the requests in flight, so requests that
+// arrive while others run start as slots and memory free up, and their
+// kernels overlap on the device (one stream per slot). A worker uploads the
+// points (when the request brought host rows), runs the skycube or skyline
+// query, copies the result to host memory and releases the device memory.
+namespace {
+
+struct Request {
+  uint64_t ticket = 0;
+  const float* rows = nullptr;  // host rows to upload, or
+  skc_dataset* ds = nullptr;    // a resident dataset
+  uint64_t n = 0;
+  int d = 0;
+  skc_options opt{};
+  uint64_t footprint = 0;
+  std::chrono::steady_clock::time_point t_submit, t_start, t_end;
+  bool done = false;
+  int status = SKC_OK;
+  std::string err;
+  skc_result* result = nullptr;
+  float device_ms = 0.f;
+};
+
+double ms_between(std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+}  // namespace
+
+struct skc_server {
+  skc_context* ctx = nullptr;
+  uint64_t budget = 0;
+  uint64_t in_use = 0;
+  int slots = 0;
+  std::vector<std::thread> workers;
+  std::vector<cudaStream_t> streams;
+  std::deque<std::shared_ptr<Request>> queue;
+  std::map<uint64_t, std::shared_ptr<Request>> tickets;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  bool stopping = false;
+  uint64_t next_ticket = 1;
+  uint64_t admitted = 0, peak_in_flight = 0, in_flight = 0;
+};
+
+// Estimated device memory of one request: the resident points, the full-space
+// pipeline, and the bitmap or per-cuboid stage with every point a candidate
+// (an upper bound of the candidates), plus room for the id lists.
+static uint64_t footprint_estimate(uint64_t n, int d, const skc_options& o, bool upload) {
+  const uint64_t np = round_up(n, 128);
+  const uint64_t W = d >= 5 ? (1ull << d) / 32 : 1;
+  uint64_t b = (uint64_t)d * np * 4;          // resident points
+  if (upload) b += n * (uint64_t)d * 4;        // staging copy
+  b += n * (16 * 3 + 4 * 8) + 2 * (uint64_t)d * np * 4;  // full space
+  if (o.subspace) {
+    b += n * (16 * 2 + 4 * 6) + 2 * (uint64_t)d * np * 4;
+  } else if (o.algo == SKC_ALGO_SDSC && o.mode == SKC_MODE_PLAIN) {
+    b += n * (16 * 2 + 4 * 6) + 2 * (uint64_t)d * np * 4;
+    b += 2 * n * 4 * std::min<uint64_t>(1ull << d, 64);  // per-cuboid lists
+  } else {
+    const bool ext = o.want_extended || o.algo == SKC_ALGO_SDSC;
+    b += 2 * (uint64_t)d * np * 4 + n * (16 * 3 + 4 * 3);
+    b += n * W * 4 * (ext ? 3 : 2);  // bitmaps + compaction
+    b += n * 4 * std::min<uint64_t>(1ull << d, 64);  // id lists
+  }
+  return b;
+}
+
+// Copies a result's lists (and bitmaps) to host memory and frees its device
+// memory, so later accessors are host lookups.
+static int result_to_host(skc_result* r) {
+  SKC_TRY(download_csr(r, false));
+  if (r->d_eoff) SKC_TRY(download_csr(r, true));
+  if (r->d_bits) {
+    const uint32_t* b;
+    const uint32_t* p;
+    uint64_t n;
+    uint32_t w;
+    SKC_TRY(skc_result_bitmaps(r, &b, &p, &n, &w));
+  }
+  cudaStream_t s = r->stream;
+  release_result_memory(r);
+  SKC_CUDA(cudaStreamSynchronize(s));
+  return SKC_OK;
+}
+
+static void serve_one(skc_server* S, cudaStream_t stream, Request& q) {
+  clear_error();
+  Exec E;
+  E.ctx = S->ctx;
+  E.stream = stream;
+  skc_dataset* ds = q.ds;
+  int st = SKC_OK;
+  if (!ds) st = upload_on(S->ctx, stream, q.rows, q.n, q.d, true, &ds);
+  if (st == SKC_OK) st = skycube_exec(E, ds, &q.opt, &q.result);
+  if (st == SKC_OK) st = result_to_host(q.result);
+  if (!q.ds && ds) skc_dataset_free(ds);
+  q.device_ms = E.ms;
+  q.status = st;
+  if (st != SKC_OK) {
+    q.err = g_err;
+    if (q.result) {
+      skc_result_free(q.result);
+      q.result = nullptr;
+    }
+  }
+}
+
+static void worker_loop(skc_server* S, int slot) {
+  cudaSetDevice(S->ctx->device);
+  cudaStream_t stream = S->streams[slot];
+  for (;;) {
+    std::shared_ptr<Request> q;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_work.wait(lk, [&] {
+        return S->stopping || (!S->queue.empty() &&
+                               S->queue.front()->footprint <= S->budget - S->in_use);
+      });
+      if (S->stopping) return;
+      q = S->queue.front();
+      S->queue.pop_front();
+      S->in_use += q->footprint;
+      ++S->admitted;
+      ++S->in_flight;
+      S->peak_in_flight = std::max(S->peak_in_flight, S->in_flight);
+      q->t_start = std::chrono::steady_clock::now();
+    }
+    serve_one(S, stream, *q);
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->in_use -= q->footprint;
+      --S->in_flight;
+      q->t_end = std::chrono::steady_clock::now();
+      q->done = true;
+    }
+    S->cv_done.notify_all();
+    S->cv_work.notify_all();
+  }
+}
+
+extern "C" {
+
+int skc_server_create(skc_context* ctx, int slots, uint64_t budget, skc_server** out) {
+  clear_error();
+  if (!ctx || !out) return set_error(SKC_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (slots < 1 || slots > 64) return set_error(SKC_ERR_INVALID, "slots=%d outside [1,64]", slots);
+  SKC_CUDA(cudaSetDevice(ctx->device));
+  if (budget == 0) {
+    size_t free_b = 0, total_b = 0;
+    SKC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    budget = (uint64_t)(free_b * 0.8);
+  }
+  auto* S = new skc_server;
+  S->ctx = ctx;
+  S->budget = budget;
+  S->slots = slots;
+  for (int i = 0; i < slots; ++i) {
+    cudaStream_t st;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+      for (auto x : S->streams) cudaStreamDestroy(x);
+      delete S;
+      return set_error(SKC_ERR_CUDA, "stream creation failed");
+    }
+    S->streams.push_back(st);
+  }
+  for (int i = 0; i < slots; ++i) S->workers.emplace_back(worker_loop, S, i);
+  *out = S;
+  return SKC_OK;
+}
+
+static int submit_common(skc_server* S, std::shared_ptr<Request> q, uint64_t* ticket) {
+  if (q->footprint > S->budget)
+    return set_error(SKC_ERR_REJECTED,
+                     "request needs about %.1f MiB of device memory, above the serving budget of %.1f MiB",
+                     q->footprint / 1048576.0, S->budget / 1048576.0);
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->stopping) return set_error(SKC_ERR_INVALID, "server is shutting down");
+    q->ticket = S->next_ticket++;
+    q->t_submit = std::chrono::steady_clock::now();
+    S->tickets[q->ticket] = q;
+    S->queue.push_back(q);
+  }
+  S->cv_work.notify_all();
+  *ticket = q->ticket;
+  return SKC_OK;
+}
+
+int skc_server_submit(skc_server* S, const float* rows, uint64_t n, int d, const skc_options* opt,
+                      uint64_t* ticket) {
+  clear_error();
+  if (!S || !rows || !ticket) return set_error(SKC_ERR_INVALID, "NULL argument");
+  if (d < SKC_MIN_DIMS || d > SKC_MAX_DIMS)
+    return set_error(SKC_ERR_INVALID, "d=%d outside [%d,%d]", d, SKC_MIN_DIMS, SKC_MAX_DIMS);
+  if (n == 0) return set_error(SKC_ERR_INVALID, "empty dataset (n=0)");
+  auto q = std::make_shared<Request>();
+  q->rows = rows;
+  q->n = n;
+  q->d = d;
+  skc_options_init(&q->opt);
+  if (opt) q->opt = *opt;
+  if (q->opt.subspace >= (1u << d))
+    return set_error(SKC_ERR_INVALID, "subspace 0x%x has attributes beyond d=%d", q->opt.subspace, d);
+  q->footprint = footprint_estimate(n, d, q->opt, true);
+  return submit_common(S, q, ticket);
+}
+
+int skc_server_submit_dataset(skc_server* S, skc_dataset* ds, const skc_options* opt,
+                              uint64_t* ticket) {
+  clear_error();
+  if (!S || !ds || !ticket) return set_error(SKC_ERR_INVALID, "NULL argument");
+  if (ds->ctx != S->ctx) return set_error(SKC_ERR_INVALID, "dataset belongs to another context");
+  auto q = std::make_shared<Request>();
+  q->ds = ds;
+  q->n = ds->n;
+  q->d = ds->d;
+  skc_options_init(&q->opt);
+  if (opt) q->opt = *opt;
+  q->footprint = footprint_estimate(ds->n, ds->d, q->opt, false);
+  return submit_common(S, q, ticket);
+}
+
+int skc_server_wait(skc_server* S, uint64_t ticket, skc_result** out, skc_server_timing* t) {
+  clear_error();
+  if (!S || !out) return set_error(SKC_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  std::shared_ptr<Request> q;
+  {
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->tickets.find(ticket);
+    if (it == S->tickets.end()) return set_error(SKC_ERR_INVALID, "unknown ticket %llu", (unsigned long long)ticket);
+    q = it->second;
+    S->cv_done.wait(lk, [&] { return q->done; });
+    S->tickets.erase(it);
+  }
+  if (t) {
+    t->queued_ms = ms_between(q->t_submit, q->t_start);
+    t->run_ms = ms_between(q->t_start, q->t_end);
+    t->total_ms = ms_between(q->t_submit, q->t_end);
+    t->device_ms = q->device_ms;
+  }
+  if (q->status != SKC_OK) {
+    g_err = q->err;
+    return q->status;
+  }
+  *out = q->result;
+  return SKC_OK;
+}
+
+int skc_server_stats(skc_server* S, uint64_t* admitted, uint64_t* peak_in_flight,
+                     uint64_t* budget) {
+  clear_error();
+  if (!S) return set_error(SKC_ERR_INVALID, "NULL server");
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (admitted) *admitted = S->admitted;
+  if (peak_in_flight) *peak_in_flight = S->peak_in_flight;
+  if (budget) *budget = S->budget;
+  return SKC_OK;
+}
+
+int skc_server_destroy(skc_server* S) {
+  clear_error();
+  if (!S) return SKC_OK;
+  {
+    // Let queued and running requests finish first.
+    std::unique_lock<std::mutex> lk(S->mu);
+    S->cv_done.wait(lk, [&] { return S->queue.empty() && S->in_flight == 0; });
+    S->stopping = true;
+  }
+  S->cv_work.notify_all();
+  for (auto& w : S->workers) w.join();
+  for (auto& kv : S->tickets)
+    if (kv.second->result) skc_result_free(kv.second->result);
+  for (auto st : S->streams) cudaStreamDestroy(st);
+  delete S;
   return SKC_OK;
 }
 

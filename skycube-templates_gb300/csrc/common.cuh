@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <set>
 #include <string>
 #include <vector>
@@ -96,10 +97,14 @@ struct skc_context {
   std::set<skc_result*> results;
   // Per-phase device times of the last skc_skycube.
   std::vector<std::pair<std::string, float>> phases;
+  // Guards the table caches and the object registries (the serving loop
+  // runs pipelines from several host threads).
+  std::mutex mu;
 };
 
 struct skc_dataset {
   skc_context* ctx = nullptr;
+  cudaStream_t stream = nullptr;  // stream its memory was allocated on
   uint64_t n = 0;
   uint64_t n_pad = 0;  // n rounded up to a multiple of 128
   int d = 0;
@@ -108,6 +113,7 @@ struct skc_dataset {
 
 struct skc_result {
   skc_context* ctx = nullptr;
+  cudaStream_t stream = nullptr;  // stream later device work on it goes to
   int d = 0;
   int max_d = 0;
   int algo = 0;

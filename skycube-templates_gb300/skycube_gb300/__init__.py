@@ -33,10 +33,15 @@ class SkycubeError(RuntimeError):
         self.code = code
 
 
+class _Timing(ctypes.Structure):
+    _fields_ = [("queued_ms", ctypes.c_double), ("run_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double), ("device_ms", ctypes.c_float)]
+
+
 class _Options(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("mode", ctypes.c_int), ("max_d", ctypes.c_int),
                 ("depth", ctypes.c_int), ("want_extended", ctypes.c_int),
-                ("want_bitmaps", ctypes.c_int)]
+                ("want_bitmaps", ctypes.c_int), ("subspace", ctypes.c_uint32)]
 
 
 _lib = None
@@ -71,6 +76,12 @@ def lib():
         "skc_last_error": (ctypes.c_char_p, []),
         "skc_kernel_launches": (u64, []),
         "skc_last_phase": (i32, [vp, i32, P(ctypes.c_char_p), P(ctypes.c_float)]),
+        "skc_server_create": (i32, [vp, i32, u64, P(vp)]),
+        "skc_server_submit": (i32, [vp, vp, u64, i32, P(_Options), P(u64)]),
+        "skc_server_submit_dataset": (i32, [vp, vp, P(_Options), P(u64)]),
+        "skc_server_wait": (i32, [vp, u64, P(vp), P(_Timing)]),
+        "skc_server_stats": (i32, [vp, P(u64), P(u64), P(u64)]),
+        "skc_server_destroy": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -235,12 +246,66 @@ def kernel_launches():
     return int(lib().skc_kernel_launches())
 
 
+def options(algo="mdmc", mode="batched", max_d=0, depth=0, want_extended=False,
+            want_bitmaps=False, subspace=0):
+    return _Options(ALGOS[algo], MODES[mode], int(max_d), int(depth),
+                    int(bool(want_extended)), int(bool(want_bitmaps)), int(subspace))
+
+
 def skycube(ctx, ds, algo="mdmc", mode="batched", max_d=0, depth=0,
-            want_extended=False, want_bitmaps=False):
-    """Computes the skycube of a resident dataset (MDMC/SDSC ::Execute)."""
-    o = _Options(ALGOS[algo], MODES[mode], int(max_d), int(depth),
-                 int(bool(want_extended)), int(bool(want_bitmaps)))
+            want_extended=False, want_bitmaps=False, subspace=0):
+    """Computes the skycube of a resident dataset (MDMC/SDSC ::Execute), or
+    with `subspace` set, only that cuboid's skyline (a skyline query)."""
+    o = options(algo, mode, max_d, depth, want_extended, want_bitmaps, subspace)
     h = ctypes.c_void_p()
     _check(lib().skc_skycube(ctx.handle, ds.handle, ctypes.byref(o), ctypes.byref(h)))
     md = ds.d if max_d <= 0 or max_d > ds.d else max_d
     return Result(ctx, h, ds.d, md)
+
+
+class Server:
+    """Continuous-batching serving loop (skc_server_*): `slots` concurrent
+    requests, admitted in order by estimated device-memory footprint."""
+
+    def __init__(self, ctx, slots=4, budget=0):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        _check(lib().skc_server_create(ctx.handle, slots, budget, ctypes.byref(h)))
+        self.handle = h
+        self._keep = {}  # ticket -> host rows kept alive until the result is taken
+
+    def submit(self, points, **opts):
+        x = np.ascontiguousarray(points, dtype=np.float32)
+        o = options(**opts)
+        t = ctypes.c_uint64()
+        _check(lib().skc_server_submit(self.handle, x.ctypes.data_as(ctypes.c_void_p), x.shape[0],
+                                       x.shape[1], ctypes.byref(o), ctypes.byref(t)))
+        self._keep[t.value] = (x, x.shape[1], o.max_d if not o.subspace else bin(o.subspace).count("1"))
+        return t.value
+
+    def wait(self, ticket):
+        """(Result, timing dict) of a submitted request."""
+        h = ctypes.c_void_p()
+        tm = _Timing()
+        x, d, md = self._keep.pop(ticket, (None, 0, 0))
+        _check(lib().skc_server_wait(self.handle, ticket, ctypes.byref(h), ctypes.byref(tm)))
+        md = d if md <= 0 or md > d else md
+        res = Result(self.ctx, h, d, md)
+        return res, {"queued_ms": tm.queued_ms, "run_ms": tm.run_ms, "total_ms": tm.total_ms,
+                     "device_ms": tm.device_ms}
+
+    def stats(self):
+        a, p, b = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib().skc_server_stats(self.handle, ctypes.byref(a), ctypes.byref(p), ctypes.byref(b)))
+        return {"admitted": a.value, "peak_in_flight": p.value, "budget": b.value}
+
+    def close(self):
+        if self.handle:
+            lib().skc_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
