@@ -52,6 +52,12 @@ def parse_args():
     ap.add_argument("--no-plain", action="store_true", help="skip the per-cuboid form")
     ap.add_argument("--cpu-sample", type=int, default=0, help="points in the CPU sample (0: auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--serving-queries", type=int, default=600,
+                    help="queries of the serving stream (0: skip serving)")
+    ap.add_argument("--serving-rate", type=float, default=40.0, help="Poisson arrival rate, queries/s")
+    ap.add_argument("--serving-slots", type=int, default=4)
+    ap.add_argument("--serving-baseline", type=int, default=60,
+                    help="queries served one at a time with the plain form for comparison")
     return ap.parse_args()
 
 
@@ -166,6 +172,82 @@ def flush_l2(buf):
     buf.zero_()
 
 
+def percentile(v, p):
+    v = sorted(v)
+    if not v:
+        return None
+    k = (len(v) - 1) * p / 100.0
+    lo, hi = int(k), min(int(k) + 1, len(v) - 1)
+    return v[lo] + (v[hi] - v[lo]) * (k - lo)
+
+
+def run_serving(sk, ctx, args):
+    """Serving stream: queries arrive Poisson at --serving-rate, each over its
+    own seeded dataset (n log-uniform in [1e3, 1e6], d in 4..16, uniform /
+    correlated / anticorrelated); half capped skycubes (<= 4 attributes), half
+    skylines of one random subspace. Served by the continuous-batching server
+    (host rows in, host results out). The first --serving-baseline queries
+    are also served one at a time with the plain per-cuboid form on the same
+    arrival times (sequential queue on a virtual clock from measured service
+    times)."""
+    stream = datagen.serving_stream(count=args.serving_queries, rate_qps=args.serving_rate, seed=7)
+    data = [datagen.generate(q["kind"], q["n"], q["d"], q["seed"]) for q in stream]
+    srv = sk.Server(ctx, slots=args.serving_slots)
+    for x, q in list(zip(data, stream))[:8]:  # warm-up (kernels, pools)
+        r, _ = srv.wait(srv.submit(x, max_d=q["max_d"], subspace=q["subspace"]))
+        r.close()
+    t0 = time.perf_counter()
+    tickets = []
+    for q, x in zip(stream, data):
+        delay = t0 + q["arrival_s"] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        tickets.append(srv.submit(x, max_d=q["max_d"], subspace=q["subspace"]))
+    lat, queued, run = [], [], []
+    for t in tickets:
+        r, tm = srv.wait(t)
+        lat.append(tm["total_ms"])
+        queued.append(tm["queued_ms"])
+        run.append(tm["run_ms"])
+        r.close()
+    span = max(time.perf_counter() - t0, stream[-1]["arrival_s"])
+    stats = srv.stats()
+    srv.close()
+    out = {"queries": len(stream), "rate_qps": args.serving_rate, "slots": args.serving_slots,
+           "p50_ms": round(percentile(lat, 50), 3), "p99_ms": round(percentile(lat, 99), 3),
+           "mean_ms": round(sum(lat) / len(lat), 3), "max_ms": round(max(lat), 3),
+           "qps": round(len(stream) / span, 2), "peak_in_flight": stats["peak_in_flight"],
+           "queued_p50_ms": round(percentile(queued, 50), 3),
+           "queued_p99_ms": round(percentile(queued, 99), 3),
+           "run_p50_ms": round(percentile(run, 50), 3), "run_p99_ms": round(percentile(run, 99), 3),
+           "form": "batched (bitmap) form, continuous batching over CUDA-stream slots"}
+    nb = min(args.serving_baseline, len(stream))
+    if nb:
+        def one_at_a_time(mode):
+            end, lats = 0.0, []
+            for q, x in list(zip(stream, data))[:nb]:
+                s0 = time.perf_counter()
+                ds = sk.Dataset(ctx, x)
+                r = sk.skycube(ctx, ds, "sdsc" if mode == "plain" else "mdmc", mode,
+                               max_d=q["max_d"], subspace=q["subspace"])
+                r.download()
+                r.close()
+                ds.close()
+                service = time.perf_counter() - s0
+                start = max(q["arrival_s"], end)
+                end = start + service
+                lats.append((end - q["arrival_s"]) * 1000.0)
+            return {"queries": nb, "p50_ms": round(percentile(lats, 50), 3),
+                    "p99_ms": round(percentile(lats, 99), 3),
+                    "qps": round(nb / max(end, stream[nb - 1]["arrival_s"]), 2)}
+        out["one_at_a_time_plain"] = one_at_a_time("plain")
+        out["one_at_a_time_batched"] = one_at_a_time("batched")
+        sub = lat[:nb]
+        out["first_queries_concurrent"] = {"queries": nb, "p50_ms": round(percentile(sub, 50), 3),
+                                           "p99_ms": round(percentile(sub, 99), 3)}
+    return out
+
+
 def run_ours(args, world, rank, local):
     import torch
     import skycube_gb300 as sk
@@ -276,6 +358,10 @@ def run_ours(args, world, rank, local):
                          f"{dt:.2f} s; cost grows faster than linearly in n, so the full 1M "
                          f"workload runs at a lower rate on the CPU"}
 
+    serving = None
+    if rank == 0 and world == 1 and args.serving_queries > 0:
+        serving = run_serving(sk, ctx, args)
+
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(mean_ms, 3),
@@ -309,6 +395,8 @@ def run_ours(args, world, rank, local):
     }
     if plain:
         out["plain"] = plain
+    if serving:
+        out["serving"] = serving
     if rank == 0:
         print(json.dumps(out), flush=True)
     ctx.close()

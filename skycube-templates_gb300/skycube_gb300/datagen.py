@@ -76,3 +76,36 @@ CONFIGS = {
     "ties-581k-10": ("ties", 581_012, 10, 10, 42),
     "corrq-566k-15-m6": ("correlated_q", 566_268, 15, 6, 42),
 }
+
+
+def serving_stream(count=2000, rate_qps=20.0, seed=7, n_min=1_000, n_max=1_000_000,
+                   skycube_max_d=4):
+    """Queries of the serving workload, in arrival order.
+
+    Each query has its own seeded dataset: n log-uniform in [n_min, n_max],
+    d uniform in {4..16}, distribution uniform over uniform (independent),
+    correlated and anticorrelated. Half are skycube queries (every cuboid of
+    at most `skycube_max_d` attributes), half skyline queries on one random
+    subspace of at least two attributes. Arrivals are Poisson with the given
+    rate (exponential gaps). Returns a list of dicts with keys arrival_s,
+    kind, n, d, seed, max_d, subspace.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    t = 0.0
+    kinds = ("uniform", "correlated", "anticorrelated")
+    for i in range(count):
+        t += rng.exponential(1.0 / rate_qps)
+        n = int(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        d = int(rng.integers(4, 17))
+        kind = kinds[int(rng.integers(0, 3))]
+        if rng.random() < 0.5:
+            q = {"max_d": min(d, skycube_max_d), "subspace": 0}
+        else:
+            while True:
+                sub = int(rng.integers(1, 1 << d))
+                if bin(sub).count("1") >= 2:
+                    break
+            q = {"max_d": 0, "subspace": sub}
+        out.append({"arrival_s": t, "kind": kind, "n": n, "d": d, "seed": 10_000 + i, **q})
+    return out
