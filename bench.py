@@ -338,16 +338,18 @@ def run_ours(args, world, rank, local):
     achieved_gbs = alg_bytes / (kern / 1000.0) / 1e9
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     pairs = float(m) * float(m)
-    ops = pairs * (2 * d + 2)
     sm_mhz = clk.get("sm_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
-    issue_peak = 152 * 128 * sm_mhz * 1e6  # lane-ops/s: 152 SMs x 128 lanes
-    traffic = None
-    tpath = os.path.join(REPO, "profiles", "bitmap_kernel_traffic.json")
+    issue_peak = 152 * 4 * sm_mhz * 1e6  # warp instructions/s: 152 SMs x 4 schedulers
+    # Counters of the same kernel from one ncu capture of this workload
+    # (profiles/kernel_counters_<workload>.json): DRAM bytes and warp
+    # instructions per launch.
+    traffic, inst = None, None
+    tpath = os.path.join(REPO, "profiles", f"kernel_counters_{args.workload}.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            t = json.load(f)
-        if t.get("workload") == args.workload:
-            traffic = t.get("dram_bytes_per_launch")
+            t = json.load(f).get("k_bitmaps", {})
+        traffic = t.get("dram_bytes_per_launch")
+        inst = t.get("warp_inst_per_launch")
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -380,12 +382,17 @@ def run_ours(args, world, rank, local):
                      "peak": hbm, "unit": "GB/s", "frac": round(achieved_gbs / hbm, 6),
                      "traffic": traffic, "peak_source": peak_kind,
                      "kernel_ms": round(kern, 3), "alg_bytes": alg_bytes},
-        "issue_roofline": {"kernel": "k_bitmaps", "achieved": round(ops / (kern / 1000.0) / 1e9, 1),
-                           "peak": round(issue_peak / 1e9, 1), "unit": "Gop/s",
-                           "frac": round(ops / (kern / 1000.0) / issue_peak, 4),
-                           "pairs": int(pairs), "ops_per_pair": 2 * d + 2,
-                           "note": "pairs = candidates^2, each costing d <= and d == compares "
-                                   "plus 2 mask ops; peak = 152 SMs x 128 lanes x median SM clock"},
+        "issue_roofline": {
+            "kernel": "k_bitmaps",
+            "achieved": round(inst / (kern / 1000.0) / 1e9, 2) if inst else None,
+            "peak": round(issue_peak / 1e9, 2), "unit": "G warp-instructions/s",
+            "frac": round(inst / (kern / 1000.0) / issue_peak, 4) if inst else None,
+            "warp_inst_per_launch": inst,
+            "pair_space": int(pairs),
+            "note": "the kernel is bound by instruction issue, not DRAM: warp instructions "
+                    "per launch from one ncu capture of this workload, divided by the live "
+                    "event-timed kernel duration; peak = 152 SMs x 4 schedulers x median SM "
+                    "clock under load"},
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": int(launches),
