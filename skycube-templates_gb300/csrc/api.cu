@@ -226,7 +226,8 @@ static int run_full_space(Exec& E, skc_dataset* ds, int depth, Arena& A,
     SKC_TRY(A.alloc(&ps.pdone, K));
   }
   SKC_TRY(A.alloc(&ps.counts, K + 1));
-  SKC_TRY(A.alloc(&ps.cursor, K + 1));
+  SKC_TRY(A.alloc(&ps.cursor, kMaxSortBuckets + 1));
+  SKC_TRY(A.alloc(&ps.fine, kMaxSortBuckets + 1));
   SKC_TRY(A.alloc(&ps.items, K + 1));
   uint8_t* status;
   SKC_TRY(A.alloc(&status, n));
@@ -415,7 +416,8 @@ static int run_sdsc_plain(Exec& E, skc_dataset* ds, int max_d,
     SKC_TRY(A.alloc(&ps.pdone, Kmax));
   }
   SKC_TRY(A.alloc(&ps.counts, Kmax + 1));
-  SKC_TRY(A.alloc(&ps.cursor, Kmax + 1));
+  SKC_TRY(A.alloc(&ps.cursor, kMaxSortBuckets + 1));
+  SKC_TRY(A.alloc(&ps.fine, kMaxSortBuckets + 1));
   SKC_TRY(A.alloc(&ps.items, Kmax + 1));
   uint32_t *cand, *d_m, *blk0, *blk1, *cnt;
   uint8_t* status;
@@ -752,7 +754,8 @@ static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, int depth,
     SKC_TRY(A.alloc(&ps.ccells, m));
     SKC_TRY(A.alloc(&ps.cx, (uint64_t)d * round_up(m, 128)));
     SKC_TRY(A.alloc(&ps.counts, K + 1));
-    SKC_TRY(A.alloc(&ps.cursor, K + 1));
+    SKC_TRY(A.alloc(&ps.cursor, kMaxSortBuckets + 1));
+    SKC_TRY(A.alloc(&ps.fine, kMaxSortBuckets + 1));
     SKC_TRY(A.alloc(&ps.items, K + 1));
     if (m >= kConfirmedMinPoints) {
       SKC_TRY(A.alloc(&ps.conf_cells, m));

@@ -79,6 +79,7 @@ int launch_skyline(cudaStream_t s, int d, const SkylineArgs& a);
 // level order.
 constexpr int kMaxPartitionDims = 10;
 constexpr uint64_t kConfirmedMinPoints = 32768;
+constexpr uint64_t kMaxSortBuckets = 1u << 18;  // partition x strength buckets
 struct LevelTables {
   int B = 0;
   const uint32_t* rank = nullptr;      // [2^B]
@@ -98,7 +99,8 @@ struct PartScratch {
   uint32_t* ccount = nullptr;   // [2^B]
   uint32_t* pdone = nullptr;    // [2^B]
   uint32_t* counts;  // [2^B + 1] partition offsets after the sort
-  uint32_t* cursor;  // [2^B + 1]
+  uint32_t* fine;    // [kMaxSortBuckets + 1] counting-sort offsets
+  uint32_t* cursor;  // [kMaxSortBuckets + 1]
   uint32_t* items;   // [2^B + 1]
 };
 struct PartitionSkylineArgs {

@@ -22,29 +22,47 @@
 namespace skc {
 
 // key[i] = rank of the median mask of list entry i over the first B
-// attributes of S.
+// attributes of S, times 2^sub_bits, plus (when sub_bits > 0) the sum of its
+// grid cells over S scaled to sub_bits bits. Sorting by the key groups
+// points by partition and, inside a partition, from strong to weak, so
+// points that survive long share warps. Only the partition part matters for
+// correctness.
 __global__ void k_mask_keys(const uint4* __restrict__ cells,
                             const uint32_t* __restrict__ ids,
                             const uint32_t* __restrict__ m_ptr, uint32_t S,
-                            int d, int B, int depth,
+                            int d, int B, int depth, int sub_bits,
                             const uint32_t* __restrict__ rank,
                             uint32_t* __restrict__ keys) {
   const uint32_t m = *m_ptr;
   const int sh = depth - 1;
+  const uint32_t cmax = (1u << depth) - 1;
+  const uint32_t span = cmax * (uint32_t)__popc(S);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m;
        i += gridDim.x * blockDim.x) {
     const uint32_t id = ids ? ids[i] : i;
     const uint4 c = cells[id];
-    uint32_t cm = 0;
+    uint32_t cm = 0, csum = 0;
     int j = 0;
-    for (int k = 0; k < d && j < B; ++k) {
+    for (int k = 0; k < d; ++k) {
       if (!(S & (1u << k))) continue;
       const uint32_t cell = (word_of(c, k >> 2) >> (8 * (k & 3))) & 0x7fu;
-      cm |= ((cell >> sh) & 1u) << j;
+      if (j < B) cm |= ((cell >> sh) & 1u) << j;
+      csum += cell;
       ++j;
     }
-    keys[i] = rank[cm];
+    uint32_t key = rank[cm] << sub_bits;
+    if (sub_bits && span) key |= (csum * ((1u << sub_bits) - 1)) / span;
+    keys[i] = key;
   }
+}
+
+// boff[b] = offsets[b << sub_bits] for b in [0, K]: partition offsets out of
+// the finer counting-sort offsets.
+__global__ void k_partition_offsets(const uint32_t* __restrict__ offsets, uint32_t K,
+                                    int sub_bits, uint32_t* __restrict__ boff) {
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b <= K;
+       b += gridDim.x * blockDim.x)
+    boff[b] = offsets[(uint64_t)b << sub_bits];
 }
 
 // items[b] = number of 256-point work items of partition b.
@@ -265,7 +283,7 @@ int launch_mask_keys(cudaStream_t s, const uint4* cells, const uint32_t* ids,
                      const uint32_t* m_ptr, uint64_t m_max, uint32_t S, int d,
                      int B, int depth, const uint32_t* rank, uint32_t* keys) {
   k_mask_keys<<<blocks_for(m_max, 256, 152 * 8), 256, 0, s>>>(cells, ids, m_ptr, S, d, B, depth,
-                                                               rank, keys);
+                                                               0, rank, keys);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }
@@ -282,14 +300,21 @@ int launch_partition_skyline(cudaStream_t s, int d, int depth,
                              const PartScratch& ps) {
   const uint32_t K = 1u << T.B;
   const int na = __builtin_popcount(a.S);
+  // Strength order inside partitions: as many cell-sum levels as keep the
+  // counting sort at <= kMaxSortBuckets buckets.
+  int sub_bits = 0;
+  while (sub_bits < 8 && ((uint64_t)K << (sub_bits + 1)) <= kMaxSortBuckets) ++sub_bits;
+  const uint32_t KB = K << sub_bits;
   BucketScratch bs;
   bs.keys = ps.keys;
-  bs.counts = ps.counts;
+  bs.counts = ps.fine;
   bs.cursor = ps.cursor;
   k_mask_keys<<<blocks_for(a.m_max, 256, 152 * 8), 256, 0, s>>>(
-      a.cells, a.ids, a.m_ptr, a.S, d, T.B, depth, T.rank, ps.keys);
+      a.cells, a.ids, a.m_ptr, a.S, d, T.B, depth, sub_bits, T.rank, ps.keys);
   SKC_LAUNCH_CHECK();
-  SKC_TRY(launch_counting_sort(s, ps.keys, a.m_ptr, a.m_max, K, bs, ps.sorted, nullptr));
+  SKC_TRY(launch_counting_sort(s, ps.keys, a.m_ptr, a.m_max, KB, bs, ps.sorted, nullptr));
+  k_partition_offsets<<<blocks_for(K + 1, 256, 64), 256, 0, s>>>(ps.fine, K, sub_bits, ps.counts);
+  SKC_LAUNCH_CHECK();
   const uint64_t pitch = (a.m_max + 127) / 128 * 128;
   k_gather_compact<<<blocks_for(a.m_max, 256, 152 * 8), 256, 0, s>>>(
       a.cells, a.x, a.n_pad, a.ids, ps.sorted, a.m_ptr, a.S, d, pitch, ps.ccells, ps.cx);
