@@ -283,16 +283,25 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   // lattice-level order (strongest partitions first).
   LevelTables LT;
   SKC_TRY(level_tables(ctx, bitmap_partition_dims(d, m), &LT));
+  // Inside a partition, q's go from strong to weak (cell sum), which keeps
+  // the 32-q blocks compact and their minimum-cell boxes tight.
   const uint32_t K = 1u << LT.B;
+  int sub_bits = 0;
+  while (sub_bits < 8 && ((uint64_t)K << (sub_bits + 1)) <= kMaxSortBuckets) ++sub_bits;
+  const uint32_t KB = K << sub_bits;
   BucketScratch b;
+  uint32_t* boff;
   SKC_TRY(A.alloc(&b.keys, m));
-  SKC_TRY(A.alloc(&b.counts, K + 1));
-  SKC_TRY(A.alloc(&b.cursor, K + 1));
+  SKC_TRY(A.alloc(&b.counts, KB + 1));
+  SKC_TRY(A.alloc(&b.cursor, KB + 1));
+  SKC_TRY(A.alloc(&boff, K + 1));
   uint32_t *qperm, *qids;
   SKC_TRY(A.alloc(&qperm, m));
   SKC_TRY(A.alloc(&qids, m));
-  SKC_TRY(launch_mask_keys(s, cc, nullptr, m_ptr, m, nsub - 1, d, LT.B, depth, LT.rank, b.keys));
-  SKC_TRY(launch_counting_sort(s, b.keys, m_ptr, m, K, b, qperm, nullptr));
+  SKC_TRY(launch_mask_keys(s, cc, nullptr, m_ptr, m, nsub - 1, d, LT.B, depth, sub_bits,
+                           LT.rank, b.keys));
+  SKC_TRY(launch_counting_sort(s, b.keys, m_ptr, m, KB, b, qperm, nullptr));
+  SKC_TRY(launch_partition_offsets(s, b.counts, K, sub_bits, boff));
   SKC_TRY(launch_gather_u32(s, F.cand, qperm, m_ptr, m, qids));
   SKC_TRY(launch_gather_soa(s, ds->x, ds->n_pad, d, qids, m_ptr, m, m_pad, xq));
   SKC_TRY(launch_gather_u4(s, cc, qperm, m_ptr, m, qc));
@@ -308,7 +317,7 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   uint32_t* slab = nullptr;
   SKC_TRY(bitmap_tie_slab_words(d, ctx->num_sms, &slab_words));
   if (slab_words) SKC_TRY(A.alloc(&slab, slab_words));
-  BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, b.counts, LT.unrank, K, LT.B, depth,
+  BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, boff, LT.unrank, K, LT.B, depth,
                 m_ptr, work, 0xffffffffu, dom, ext, 0, slab};
   if (o.mode == SKC_MODE_BATCHED) {
     SKC_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), s));

@@ -115,7 +115,10 @@ struct PartitionSkylineArgs {
 };
 int launch_mask_keys(cudaStream_t s, const uint4* cells, const uint32_t* ids,
                      const uint32_t* m_ptr, uint64_t m_max, uint32_t S, int d,
-                     int B, int depth, const uint32_t* rank, uint32_t* keys);
+                     int B, int depth, int sub_bits, const uint32_t* rank,
+                     uint32_t* keys);
+int launch_partition_offsets(cudaStream_t s, const uint32_t* fine, uint32_t K, int sub_bits,
+                             uint32_t* boff);
 int launch_partition_skyline(cudaStream_t s, int d, int depth,
                              const LevelTables& T, const PartitionSkylineArgs& a,
                              const PartScratch& ps);

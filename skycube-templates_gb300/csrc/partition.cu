@@ -281,9 +281,17 @@ static inline unsigned blocks_for(uint64_t items, int threads, int cap);
 
 int launch_mask_keys(cudaStream_t s, const uint4* cells, const uint32_t* ids,
                      const uint32_t* m_ptr, uint64_t m_max, uint32_t S, int d,
-                     int B, int depth, const uint32_t* rank, uint32_t* keys) {
+                     int B, int depth, int sub_bits, const uint32_t* rank,
+                     uint32_t* keys) {
   k_mask_keys<<<blocks_for(m_max, 256, 152 * 8), 256, 0, s>>>(cells, ids, m_ptr, S, d, B, depth,
-                                                               0, rank, keys);
+                                                               sub_bits, rank, keys);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
+int launch_partition_offsets(cudaStream_t s, const uint32_t* fine, uint32_t K, int sub_bits,
+                             uint32_t* boff) {
+  k_partition_offsets<<<blocks_for(K + 1, 256, 64), 256, 0, s>>>(fine, K, sub_bits, boff);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }
