@@ -72,6 +72,7 @@ extern "C" {
 typedef struct skc_context skc_context;
 typedef struct skc_dataset skc_dataset;
 typedef struct skc_result skc_result;
+typedef struct skc_plan skc_plan;
 
 typedef struct skc_options {
   int algo;        /* SKC_ALGO_* */
@@ -82,9 +83,24 @@ typedef struct skc_options {
   int want_bitmaps;  /* keep per-point bitmaps for skc_result_bitmaps */
   uint32_t subspace; /* 0: the skycube; a cuboid mask: only that cuboid's
                         skyline and extended skyline (a skyline query) */
+  /* Work parameters: they change the work done, never the result. 0 means
+   * automatic: the value skc_autotune stored for datasets like this one
+   * (same size class, d and distribution signature), else the default. */
+  int pq_size;       /* pruners of the prefilter ahead of the full-space
+                        skyline (-q; Config::pq_size, src/utilities/config.h:20):
+                        > 0 that many, applied when n > 2 * pq_size as the
+                        suite does (src/mdmc/MDMC.cu:251); < 0 off; 0 auto
+                        (default 128 when n >= 32768) */
+  int tile_points;   /* bitmap kernel: mean q points per median partition
+                        (a power of two, 32..65536); 0 auto (256) */
+  int chunk;         /* bitmap kernel: candidates a warp takes per work-queue
+                        grab, 1..64; 0 auto (1) */
+  int blocks_per_sm; /* bitmap kernel: persistent CTAs per SM, 1..32 (capped
+                        by occupancy); 0 auto (the occupancy limit) */
 } skc_options;
 
-/* Fills *opt with defaults: MDMC, BATCHED, all cuboids, auto depth. */
+/* Fills *opt with defaults: MDMC, BATCHED, all cuboids, automatic work
+ * parameters. */
 void skc_options_init(skc_options* opt);
 
 /* Creates a context on CUDA device `device` (the -g value). */
@@ -169,6 +185,63 @@ int skc_server_stats(skc_server* srv, uint64_t* admitted,
                      uint64_t* peak_in_flight, uint64_t* budget);
 /* Waits for queued and running requests, then stops the workers. */
 int skc_server_destroy(skc_server* srv);
+
+/* ---- Plans: the batched launch sequence as one CUDA graph ----------------
+ * skc_plan_create runs skc_skycube(ctx, ds, opt) once to learn the
+ * candidate count and the id totals, allocates every buffer of the batched
+ * pipeline once (25% above those sizes), and captures the whole launch
+ * sequence (prefilter, full-space skyline, bitmap kernel, compaction, and
+ * the copy of the totals to pinned host memory) into a CUDA graph with no
+ * host synchronisation inside. skc_plan_execute replays it: one graph
+ * launch and one host synchronisation, on the dataset's current points
+ * (skc_dataset_update replaces them in place). When the points changed so
+ * much that a capacity overflows, the plan re-sizes itself, captures again
+ * and re-runs (counted by skc_plan_info). Only the BATCHED form of the
+ * skycube is planned (opt->mode must be SKC_MODE_BATCHED, opt->subspace 0).
+ * The result owns copies of the plan's outputs. A plan whose dataset was
+ * freed fails with SKC_ERR_INVALID. */
+int skc_plan_create(skc_context* ctx, skc_dataset* ds, const skc_options* opt,
+                    skc_plan** out);
+int skc_plan_execute(skc_plan* plan, skc_result** out);
+/* Kernels per replay, re-plans so far, and the capacities in use. */
+int skc_plan_info(skc_plan* plan, uint64_t* kernels, uint64_t* replans,
+                  uint64_t* cand_capacity, uint64_t* ids_capacity);
+int skc_plan_destroy(skc_plan* plan);
+
+/* Replaces the points of a resident dataset in place from HOST rows (same
+ * n and d, row-major float32); plans on it stay valid. Rows with non-finite
+ * values are rejected (SKC_ERR_INVALID) and the dataset keeps its points. */
+int skc_dataset_update(skc_dataset* ds, const float* rows);
+
+/* ---- Autotuner -----------------------------------------------------------
+ * Picks the work parameters (grid depth, prefilter pruners, bitmap tile,
+ * queue chunk, CTAs per SM) for `ds` under the options in `base`: starting
+ * from the defaults it times full runs on the device (CUDA events, the
+ * minimum of `repeats` runs, 0: 2) in one pass of coordinate search over
+ * the fields `base` leaves at 0, keeping a change when it is at least 2%
+ * faster. The winner is stored in the context under the dataset's
+ * signature key: its size class (floor(log2 n)), d, its distribution class
+ * (skc_dataset_signature) and the options' algorithm, form, cuboid cap and
+ * query kind. Later skc_skycube calls (and server requests) on datasets
+ * with the same key use it for the fields they leave at 0. *best receives
+ * `base` with every work field set to the chosen value (pq_size -1 when the
+ * prefilter lost), *best_ms its device time. The suite picks its
+ * partitioning depth by hand (-d); nothing there times alternatives. */
+int skc_autotune(skc_context* ctx, skc_dataset* ds, const skc_options* base,
+                 int repeats, skc_options* best, float* best_ms);
+/* Distribution classes of a dataset, measured once on a strided sample of
+ * up to 512 points: size_class = floor(log2 n); sky_class from the fraction
+ * f of the sample on its own skyline on a two-sided log scale,
+ * L(f) = floor(log2(1 + 1000 f)) for f <= 1/2 and 17 - L(1 - f) above, so
+ * 0..17 (at d = 8: correlated ~4, independent ~9, anticorrelated ~13; at
+ * high d independent and anticorrelated data both reach 17, and both have
+ * nearly every point as a candidate); ties = 1 when at least 1/8 of the
+ * sample shares an attribute value with another sample point. */
+int skc_dataset_signature(skc_dataset* ds, int* size_class, int* sky_class,
+                          int* ties);
+/* Number of stored tunings; forgets them all. */
+int skc_tuning_count(skc_context* ctx, uint64_t* count);
+int skc_tuning_clear(skc_context* ctx);
 
 /* Milliseconds of device time of the last skc_skycube on this context,
  * measured with CUDA events on the context's stream. */

@@ -61,16 +61,31 @@ int set_error(int code, const char* fmt, ...) {
 void clear_error() { g_err.clear(); }
 
 static std::atomic<uint64_t> g_launches{0};
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+// Launches recorded into a CUDA graph are counted when the graph runs.
+static thread_local bool t_capturing = false;
+void count_launch() {
+  if (!t_capturing) g_launches.fetch_add(1, std::memory_order_relaxed);
+}
 
 // Execution state of one pipeline run: the stream it is issued on and the
 // per-phase device times (CUDA events on that stream). skc_skycube runs on
 // the context's stream; each serving slot has its own.
+// Capacities of a plan's buffers (skc_plan): candidates and skyline /
+// extended-skyline ids. In plan mode the pipeline reads no count back to the
+// host; it sizes everything by these and leaves the true values in `stats`
+// (device): [0] candidates, [1] skyline ids, [2] extended-skyline ids.
+struct PlanCaps {
+  uint64_t m_cap = 0;
+  uint64_t ids_cap[2] = {0, 0};
+  uint64_t* stats = nullptr;
+};
+
 struct Exec {
   skc_context* ctx = nullptr;
   cudaStream_t stream = nullptr;
   std::vector<std::pair<std::string, float>> phases;
   float ms = 0.f;
+  const PlanCaps* plan = nullptr;  // plan mode (no host synchronisation)
 };
 
 // Records phase marks on the Exec's stream; fills Exec::phases when it goes
@@ -85,6 +100,7 @@ struct Tracer {
     mark("start");
   }
   void mark(const char* name) {
+    if (E.plan) return;  // plan mode: the graph is timed as a whole
     cudaEvent_t ev;
     if (cudaEventCreate(&ev) != cudaSuccess) return;
     cudaEventRecord(ev, E.stream);
@@ -107,16 +123,41 @@ struct Tracer {
 };
 
 // Owns the temporary device buffers of one call; frees them stream-ordered.
+// For a plan (skc_plan) it runs in one of two other modes: RECORD allocates
+// with cudaMalloc and keeps every buffer in *bufs (the plan owns them);
+// REPLAY hands the recorded buffers out again in the same order, so the
+// launch sequence captured into the graph allocates nothing.
 struct Arena {
+  enum Mode { STREAM, RECORD, REPLAY };
   cudaStream_t s;
   std::vector<void*> ptrs;
+  Mode mode = STREAM;
+  std::vector<std::pair<void*, size_t>>* bufs = nullptr;
+  size_t next = 0;
   explicit Arena(cudaStream_t st) : s(st) {}
+  Arena(cudaStream_t st, Mode m, std::vector<std::pair<void*, size_t>>* b)
+      : s(st), mode(m), bufs(b) {}
   ~Arena() {
-    for (void* p : ptrs) cudaFreeAsync(p, s);
+    if (mode == STREAM)
+      for (void* p : ptrs) cudaFreeAsync(p, s);
   }
   template <typename T>
   int alloc(T** p, uint64_t count) {
     const size_t bytes = (size_t)std::max<uint64_t>(count, 1) * sizeof(T);
+    if (mode == REPLAY) {
+      if (next >= bufs->size() || (*bufs)[next].second != bytes)
+        return set_error(SKC_ERR_INVALID, "plan replay does not match its recording (buffer %zu)", next);
+      *p = (T*)(*bufs)[next++].first;
+      return SKC_OK;
+    }
+    if (mode == RECORD) {
+      cudaError_t e = cudaMalloc((void**)p, bytes);
+      if (e != cudaSuccess)
+        return set_error(e == cudaErrorMemoryAllocation ? SKC_ERR_OOM : SKC_ERR_CUDA,
+                         "plan allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+      bufs->push_back({(void*)*p, bytes});
+      return SKC_OK;
+    }
     cudaError_t e = cudaMallocAsync((void**)p, bytes, s);
     if (e != cudaSuccess)
       return set_error(e == cudaErrorMemoryAllocation ? SKC_ERR_OOM : SKC_ERR_CUDA,
@@ -178,12 +219,22 @@ static int partition_dims(uint32_t S) {
 }
 
 // Partition width of the bitmap kernel's q order: as many attributes as
-// keep partitions at >= 256 points on average (at most 10, at least 1).
-static int bitmap_partition_dims(int d, uint64_t m) {
+// keep partitions at >= tile_points points on average (at most 10, at
+// least 1).
+static int bitmap_partition_dims(int d, uint64_t m, int tile_points) {
   int B = 1;
-  while (B < kMaxPartitionDims && B < d && (m >> (B + 1)) >= 256) ++B;
+  while (B < kMaxPartitionDims && B < d && (m >> (B + 1)) >= (uint64_t)tile_points) ++B;
   return B;
 }
+
+// Work parameters of one run, after defaults and stored tunings apply.
+struct RunParams {
+  int depth = kMaxDepth;
+  int pq_size = 0;        // prefilter pruners; 0: no prefilter
+  int tile_points = 256;  // bitmap kernel: mean q's per median partition
+  int chunk = 1;          // bitmap kernel: candidates per queue grab
+  int blocks_per_sm = 0;  // bitmap kernel: 0 = occupancy limit
+};
 
 // Device-side result of the full-space step.
 struct FullSpace {
@@ -195,12 +246,13 @@ struct FullSpace {
   uint32_t h_counts[3] = {0, 0, 0};
 };
 
-static int run_full_space(Exec& E, skc_dataset* ds, int depth, Arena& A,
+static int run_full_space(Exec& E, skc_dataset* ds, const RunParams& P, Arena& A,
                           FullSpace& F, Tracer& T) {
   skc_context* ctx = E.ctx;
   cudaStream_t s = E.stream;
   const uint64_t n = ds->n;
   const int d = ds->d;
+  const int depth = P.depth;
   const uint32_t full = (1u << d) - 1;
   uint32_t* d_n;
   SKC_TRY(A.alloc(&d_n, 1));
@@ -210,6 +262,33 @@ static int run_full_space(Exec& E, skc_dataset* ds, int depth, Arena& A,
   SKC_TRY(A.alloc(&F.cells, n));
   SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, nullptr, d_n, n, depth, pivots, F.cells));
   T.mark("full: pivots+cells");
+
+  // Pruner prefilter: the skyline kernel then runs over the survivors only
+  // (as point ids, ascending; their count stays on the device).
+  const uint32_t* list = nullptr;
+  const uint32_t* m_list = d_n;
+  if (P.pq_size > 0) {
+    const uint32_t Kq = (uint32_t)P.pq_size;
+    const uint64_t nb = (n + 1023) / 1024 + 1;
+    PrefilterScratch pf;
+    SKC_TRY(A.alloc(&pf.hist, prefilter_sum_bins()));
+    SKC_TRY(A.alloc(&pf.sel, 8));
+    SKC_TRY(A.alloc(&pf.pr_ids, Kq));
+    SKC_TRY(A.alloc(&pf.pr_key, Kq));
+    SKC_TRY(A.alloc(&pf.pr_cells, Kq));
+    SKC_TRY(A.alloc(&pf.pr_x, (uint64_t)d * Kq));
+    SKC_TRY(A.alloc(&pf.st, n));
+    SKC_TRY(A.alloc(&pf.blk0, nb));
+    SKC_TRY(A.alloc(&pf.blk1, nb));
+    uint32_t *surv, *d_ns;
+    SKC_TRY(A.alloc(&surv, n));
+    SKC_TRY(A.alloc(&d_ns, 1));
+    PrefilterArgs pfa{F.cells, ds->x, ds->n_pad, nullptr, d_n, n, full, Kq, pf};
+    SKC_TRY(launch_prefilter(s, d, ctx->num_sms, pfa, surv, d_ns));
+    list = surv;
+    m_list = d_ns;
+    T.mark("full: prefilter");
+  }
 
   LevelTables LT;
   SKC_TRY(level_tables(ctx, partition_dims(full), &LT));
@@ -231,7 +310,7 @@ static int run_full_space(Exec& E, skc_dataset* ds, int depth, Arena& A,
   SKC_TRY(A.alloc(&ps.items, K + 1));
   uint8_t* status;
   SKC_TRY(A.alloc(&status, n));
-  PartitionSkylineArgs pa{nullptr, F.cells, ds->x, ds->n_pad, d_n, n, full, status};
+  PartitionSkylineArgs pa{list, F.cells, ds->x, ds->n_pad, m_list, n, full, status};
   SKC_TRY(launch_partition_skyline(s, d, depth, LT, pa, ps));
   T.mark("full: skyline kernel");
 
@@ -243,10 +322,18 @@ static int run_full_space(Exec& E, skc_dataset* ds, int depth, Arena& A,
   SKC_TRY(A.alloc(&F.sky, n));
   SKC_TRY(A.alloc(&F.ext, n));
   SKC_TRY(A.alloc(&F.cand, n));
-  SKC_TRY(launch_status_compact(s, status, nullptr, d_n, n, 0, blk0, blk1, F.sky, F.ext,
+  SKC_TRY(launch_status_compact(s, status, list, m_list, n, 0, blk0, blk1, F.sky, F.ext,
                                 F.counts + 0, F.counts + 1));
-  SKC_TRY(launch_status_compact(s, status, nullptr, d_n, n, 1, blk0, blk1, F.cand, nullptr,
+  SKC_TRY(launch_status_compact(s, status, list, m_list, n, 1, blk0, blk1, F.cand, nullptr,
                                 F.counts + 2, nullptr));
+  if (E.plan) {
+    // Plan mode: candidates sized by the plan's capacity (no read-back).
+    const uint64_t cap = std::min<uint64_t>(E.plan->m_cap, n);
+    SKC_TRY(launch_cap_count(s, F.counts + 2, (uint32_t)cap, E.plan->stats, 0));
+    F.h_counts[0] = F.h_counts[1] = 0;
+    F.h_counts[2] = (uint32_t)cap;
+    return SKC_OK;
+  }
   SKC_CUDA(cudaMemcpyAsync(F.h_counts, F.counts, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   SKC_CUDA(cudaStreamSynchronize(s));
   T.mark("full: compaction");
@@ -255,11 +342,12 @@ static int run_full_space(Exec& E, skc_dataset* ds, int depth, Arena& A,
 
 // Bitmaps of every candidate, then CSR compaction (BATCHED and PLAIN/MDMC).
 static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
-                       int depth, int max_d, Arena& A, FullSpace& F,
+                       const RunParams& P, int max_d, Arena& A, FullSpace& F,
                        skc_result* R, Tracer& T) {
   skc_context* ctx = E.ctx;
   cudaStream_t s = E.stream;
   const int d = ds->d;
+  const int depth = P.depth;
   const uint32_t nsub = 1u << d;
   const uint32_t W = nsub >= 32 ? nsub / 32 : 1;
   const uint64_t m = F.h_counts[2];
@@ -282,7 +370,7 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   // q order: partitions by median mask over the first B attributes, in
   // lattice-level order (strongest partitions first).
   LevelTables LT;
-  SKC_TRY(level_tables(ctx, bitmap_partition_dims(d, m), &LT));
+  SKC_TRY(level_tables(ctx, bitmap_partition_dims(d, m, P.tile_points), &LT));
   // Inside a partition, q's go from strong to weak (cell sum), which keeps
   // the 32-q blocks compact and their minimum-cell boxes tight.
   const uint32_t K = 1u << LT.B;
@@ -318,7 +406,8 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   SKC_TRY(bitmap_tie_slab_words(d, ctx->num_sms, &slab_words));
   if (slab_words) SKC_TRY(A.alloc(&slab, slab_words));
   BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, boff, LT.unrank, K, LT.B, depth,
-                m_ptr, work, 0xffffffffu, dom, ext, 0, slab};
+                m_ptr, work, (uint32_t)P.chunk, 0xffffffffu, dom, ext,
+                P.blocks_per_sm * ctx->num_sms, slab};
   if (o.mode == SKC_MODE_BATCHED) {
     SKC_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), s));
     SKC_TRY(launch_bitmaps(s, d, ctx->num_sms, ba));
@@ -367,11 +456,19 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
     ca.csr_off = csr;
     SKC_TRY(launch_bits_count(s, ca));
     uint64_t total = 0;
-    SKC_CUDA(cudaMemcpyAsync(&total, csr + nsub, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-    SKC_CUDA(cudaStreamSynchronize(s));
+    if (E.plan) {
+      // Plan mode: ids sized by the plan's capacity; the true total goes to
+      // the stats and writes past the capacity are skipped.
+      total = E.plan->ids_cap[pass];
+      SKC_TRY(launch_stat_u64(s, csr + nsub, E.plan->stats, 1 + pass));
+    } else {
+      SKC_CUDA(cudaMemcpyAsync(&total, csr + nsub, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+      SKC_CUDA(cudaStreamSynchronize(s));
+    }
     uint32_t* ids;
     SKC_TRY(A.alloc(&ids, total));
     ca.out = ids;
+    ca.out_cap = total;
     SKC_TRY(launch_bits_write(s, ca));
     T.mark(pass == 0 ? "compaction: skylines" : "compaction: extended");
     A.release(csr);
@@ -531,12 +628,173 @@ static int auto_depth(uint64_t n, int d) {
   return kMaxDepth;
 }
 
+// Defaults of the work parameters (used when neither the options nor a
+// stored tuning set them).
+constexpr int kDefaultPruners = 128;             // the suite's -q default
+constexpr uint64_t kPrefilterMinPoints = 32768;  // below: launch-bound anyway
+constexpr int kDefaultTilePoints = 256;
+
+// The dataset's sample signature (computed once, on stream s).
+static int dataset_signature(skc_dataset* ds, cudaStream_t s, uint32_t sig[3]) {
+  skc_context* ctx = ds->ctx;
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (ds->sig_ready) {
+      sig[0] = ds->sig_samples;
+      sig[1] = ds->sig_sky;
+      sig[2] = ds->sig_tied;
+      return SKC_OK;
+    }
+  }
+  uint32_t h[3] = {0, 0, 0};
+  {
+    Arena A(s);
+    uint32_t* out;
+    SKC_TRY(A.alloc(&out, 3));
+    SKC_TRY(launch_sample_signature(s, ds->x, ds->n_pad, ds->n, ds->d, out));
+    SKC_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SKC_CUDA(cudaStreamSynchronize(s));
+  }
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ds->sig_samples = h[2];
+  ds->sig_sky = h[0];
+  ds->sig_tied = h[1];
+  ds->sig_ready = true;
+  sig[0] = h[2];
+  sig[1] = h[0];
+  sig[2] = h[1];
+  return SKC_OK;
+}
+
+// floor(log2(1 + 1000 * f)) for f in [0, 1]: 0..9.
+static int log_class(double f) {
+  int c = 0;
+  while (c < 9 && (double)(2u << c) <= 1.0 + 1000.0 * f) ++c;
+  return c;
+}
+
+// Classes of a signature: size = floor(log2 n); sky = a two-sided log scale
+// of the sample skyline fraction f, fine near 0 (correlated data) and near 1
+// (anticorrelated or high-d data): log_class(f) for f <= 1/2, else
+// 17 - log_class(1 - f), so 0..17; ties = at least 1/8 of the sample shares
+// a value with another sample point.
+static void signature_classes(const skc_dataset* ds, const uint32_t sig[3], int* size_class,
+                              int* sky_class, int* ties) {
+  int sc = 0;
+  while (sc < 63 && (ds->n >> (sc + 1))) ++sc;
+  const double f = sig[0] ? (double)sig[1] / sig[0] : 0.0;
+  *size_class = sc;
+  *sky_class = f <= 0.5 ? log_class(f) : 17 - log_class(1.0 - f);
+  *ties = sig[0] && sig[2] * 8 >= sig[0];
+}
+
+// Tuning-table key: the dataset's classes, d, and the options that shape
+// the pipeline (algorithm, form, cuboid cap, skyline query or skycube).
+static uint64_t tuning_key(const skc_dataset* ds, const uint32_t sig[3], const skc_options& o,
+                           int max_d) {
+  int sc, kc, ties;
+  signature_classes(ds, sig, &sc, &kc, &ties);
+  uint64_t k = (uint64_t)sc;           // bits 0-5
+  k |= (uint64_t)ds->d << 6;           // bits 6-10
+  k |= (uint64_t)kc << 11;             // bits 11-15
+  k |= (uint64_t)ties << 16;
+  k |= (uint64_t)(o.algo & 1) << 17;
+  k |= (uint64_t)(o.mode & 1) << 18;
+  k |= (uint64_t)max_d << 19;          // bits 19-23
+  k |= (uint64_t)(o.subspace != 0) << 24;
+  return k;
+}
+
+// Work parameters of a run: explicit options first, then the stored tuning
+// for the dataset's signature (looked up only when some field is automatic
+// and the table is not empty), then the defaults.
+static int resolve_params(skc_dataset* ds, cudaStream_t s, const skc_options& o, int max_d,
+                          RunParams* out) {
+  skc_context* ctx = ds->ctx;
+  const uint64_t n = ds->n;
+  const bool any_auto = !o.depth || !o.pq_size || !o.tile_points || !o.chunk || !o.blocks_per_sm;
+  bool have = false;
+  skc_context::Tuned tv{};
+  bool table = false;
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    table = !ctx->tunings.empty();
+  }
+  if (any_auto && table) {
+    uint32_t sig[3];
+    SKC_TRY(dataset_signature(ds, s, sig));
+    const uint64_t key = tuning_key(ds, sig, o, max_d);
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto it = ctx->tunings.find(key);
+    if (it != ctx->tunings.end()) {
+      tv = it->second;
+      have = true;
+    }
+  }
+  RunParams P;
+  P.depth = o.depth ? o.depth : have ? tv.depth : auto_depth(n, ds->d);
+  int pq = 0;
+  if (o.pq_size > 0) pq = o.pq_size;
+  else if (o.pq_size == 0) pq = have ? tv.pq_size : (n >= kPrefilterMinPoints ? kDefaultPruners : 0);
+  P.pq_size = (pq > 0 && n > 2ull * (uint64_t)pq) ? pq : 0;
+  P.tile_points = o.tile_points ? o.tile_points : have ? tv.tile_points : kDefaultTilePoints;
+  P.chunk = o.chunk ? o.chunk : have ? tv.chunk : 1;
+  P.blocks_per_sm = o.blocks_per_sm ? o.blocks_per_sm : have ? tv.blocks_per_sm : 0;
+  *out = P;
+  return SKC_OK;
+}
+
 }  // namespace skc
 
 using namespace skc;
 
 // Frees an object's device memory and detaches it from its context; the host
 // struct stays valid until the caller frees it.
+// A captured batched pipeline (skc_plan_*): the plan owns every buffer of the
+// pipeline (Arena RECORD mode) and a CUDA graph of its launch sequence.
+struct skc_plan {
+  skc_context* ctx = nullptr;
+  skc_dataset* ds = nullptr;  // nullptr once the dataset was freed
+  skc_options opt{};
+  RunParams P;
+  int max_d = 0;
+  PlanCaps caps;
+  std::vector<std::pair<void*, size_t>> bufs;
+  skc_result outs;              // device views of the graph's outputs
+  uint64_t* h_stats = nullptr;  // pinned copy of caps.stats
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t kernels = 0;  // kernel nodes of the graph
+  uint64_t replans = 0;
+};
+
+static void plan_release_device(skc_plan* p) {
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = nullptr;
+  p->graph = nullptr;
+  for (auto& b : p->bufs) cudaFree(b.first);
+  p->bufs.clear();
+  p->caps.stats = nullptr;
+  p->kernels = 0;
+  p->outs.d_off = p->outs.d_eoff = nullptr;
+  p->outs.d_ids = p->outs.d_eids = p->outs.d_bits = p->outs.d_cand = nullptr;
+}
+
+// Frees a plan's device state and unregisters it (the object stays).
+static void release_plan_memory(skc_plan* p) {
+  if (!p->ctx) return;
+  plan_release_device(p);
+  if (p->h_stats) cudaFreeHost(p->h_stats);
+  p->h_stats = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(p->ctx->mu);
+    p->ctx->plans.erase(p);
+  }
+  p->ctx = nullptr;
+  p->ds = nullptr;
+}
+
 static void release_result_memory(skc_result* r) {
   if (!r->ctx) return;
   cudaStream_t s = r->stream ? r->stream : r->ctx->stream;
@@ -563,6 +821,8 @@ static void release_dataset_memory(skc_dataset* ds) {
   {
     std::lock_guard<std::mutex> lock(ds->ctx->mu);
     ds->ctx->datasets.erase(ds);
+    for (skc_plan* p : ds->ctx->plans)
+      if (p->ds == ds) p->ds = nullptr;  // its graph reads ds->x: never again
   }
   ds->ctx = nullptr;
 }
@@ -594,6 +854,10 @@ void skc_options_init(skc_options* o) {
   o->want_extended = 0;
   o->want_bitmaps = 0;
   o->subspace = 0;
+  o->pq_size = 0;
+  o->tile_points = 0;
+  o->chunk = 0;
+  o->blocks_per_sm = 0;
 }
 
 int skc_context_create(int device, skc_context** out) {
@@ -628,6 +892,8 @@ int skc_context_destroy(skc_context* ctx) {
   if (!ctx) return SKC_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  for (skc_plan* p : std::vector<skc_plan*>(ctx->plans.begin(), ctx->plans.end()))
+    release_plan_memory(p);
   for (skc_result* r : std::vector<skc_result*>(ctx->results.begin(), ctx->results.end()))
     release_result_memory(r);
   for (skc_dataset* ds : std::vector<skc_dataset*>(ctx->datasets.begin(), ctx->datasets.end()))
@@ -738,6 +1004,17 @@ static int check_options(skc_dataset* ds, const skc_options* opt, skc_options* o
     return set_error(SKC_ERR_INVALID, "depth %d outside [1,%d] (0 = auto)", o->depth, kMaxDepth);
   if (o->subspace >= (1u << ds->d))
     return set_error(SKC_ERR_INVALID, "subspace 0x%x has attributes beyond d=%d", o->subspace, ds->d);
+  if (o->pq_size > kMaxPruners)
+    return set_error(SKC_ERR_INVALID, "pq_size %d above %d", o->pq_size, kMaxPruners);
+  if (o->tile_points != 0 &&
+      (o->tile_points < 32 || o->tile_points > 65536 || (o->tile_points & (o->tile_points - 1))))
+    return set_error(SKC_ERR_INVALID, "tile_points %d is not a power of two in [32, 65536]",
+                     o->tile_points);
+  if (o->chunk < 0 || o->chunk > 64)
+    return set_error(SKC_ERR_INVALID, "chunk %d outside [1, 64] (0 = auto)", o->chunk);
+  if (o->blocks_per_sm < 0 || o->blocks_per_sm > 32)
+    return set_error(SKC_ERR_INVALID, "blocks_per_sm %d outside [1, 32] (0 = auto)",
+                     o->blocks_per_sm);
   return SKC_OK;
 }
 
@@ -818,15 +1095,21 @@ static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, int depth,
 
 // Runs one skycube (or skyline query) on E's stream; on success *out is a
 // new result registered with the context.
-static int skycube_exec(Exec& E, skc_dataset* ds, const skc_options* opt, skc_result** out) {
+// `forced`, when given, replaces the resolution of the work parameters (the
+// autotuner's trials).
+static int skycube_exec(Exec& E, skc_dataset* ds, const skc_options* opt, skc_result** out,
+                        const RunParams* forced = nullptr) {
   skc_context* ctx = E.ctx;
   skc_options o;
   SKC_TRY(check_options(ds, opt, &o));
   const int d = ds->d;
   const int max_d = (o.max_d <= 0 || o.max_d > d) ? d : o.max_d;
-  const int depth = o.depth ? o.depth : auto_depth(ds->n, d);
   SKC_CUDA(cudaSetDevice(ctx->device));
   cudaStream_t s = E.stream;
+  RunParams P;
+  if (forced) P = *forced;
+  else SKC_TRY(resolve_params(ds, s, o, max_d, &P));
+  const int depth = P.depth;
 
   auto* R = new skc_result;
   R->ctx = ctx;
@@ -839,7 +1122,7 @@ static int skycube_exec(Exec& E, skc_dataset* ds, const skc_options* opt, skc_re
     Arena A(s);
     FullSpace F;
     Tracer T(E);
-    st = run_full_space(E, ds, depth, A, F, T);
+    st = run_full_space(E, ds, P, A, F, T);
     if (st == SKC_OK) {
       R->n_cand = F.h_counts[2];
       if (o.subspace) {
@@ -847,7 +1130,7 @@ static int skycube_exec(Exec& E, skc_dataset* ds, const skc_options* opt, skc_re
       } else if (o.algo == SKC_ALGO_SDSC && o.mode == SKC_MODE_PLAIN) {
         st = run_sdsc_plain(E, ds, max_d, depth, A, F, R, T);
       } else {
-        st = run_bitmaps(E, ds, o, depth, max_d, A, F, R, T);
+        st = run_bitmaps(E, ds, o, P, max_d, A, F, R, T);
       }
     }
     T.mark("end");
@@ -882,6 +1165,390 @@ int skc_skycube(skc_context* ctx, skc_dataset* ds, const skc_options* opt, skc_r
   ctx->phases = E.phases;
   ctx->last_ms = E.ms;
   return st;
+}
+
+}  // extern "C"
+
+// The batched pipeline in plan mode on stream s: RECORD runs it eagerly and
+// allocates the plan's buffers, REPLAY re-issues the identical launch
+// sequence on those buffers (inside a stream capture).
+static int plan_pipeline(skc_plan* p, Arena::Mode mode, cudaStream_t s) {
+  Exec E;
+  E.ctx = p->ctx;
+  E.stream = s;
+  E.plan = &p->caps;
+  Arena A(s, mode, &p->bufs);
+  SKC_TRY(A.alloc(&p->caps.stats, 4));
+  FullSpace F;
+  Tracer T(E);
+  skc_result& R = p->outs;
+  R.d = p->ds->d;
+  R.max_d = p->max_d;
+  R.algo = p->opt.algo;
+  SKC_TRY(run_full_space(E, p->ds, p->P, A, F, T));
+  SKC_TRY(run_bitmaps(E, p->ds, p->opt, p->P, p->max_d, A, F, &R, T));
+  SKC_CUDA(cudaMemcpyAsync(p->h_stats, p->caps.stats, 3 * sizeof(uint64_t),
+                           cudaMemcpyDeviceToHost, s));
+  return SKC_OK;
+}
+
+static bool plan_fits(const skc_plan* p) {
+  const bool ext = p->outs.d_eids != nullptr;
+  return p->h_stats[0] <= p->caps.m_cap && p->h_stats[1] <= p->caps.ids_cap[0] &&
+         (!ext || p->h_stats[2] <= p->caps.ids_cap[1]);
+}
+
+static uint64_t with_slack(uint64_t v) { return v + v / 4 + 1024; }
+
+// Sizes the plan's buffers, records them with an eager run (growing the
+// capacities until that run fits), then captures the launch sequence.
+static int plan_build(skc_plan* p, uint64_t m_cap, uint64_t ids0, uint64_t ids1) {
+  cudaStream_t s = p->ctx->stream;
+  for (int tries = 0;; ++tries) {
+    plan_release_device(p);
+    p->caps.m_cap = std::min<uint64_t>(m_cap, p->ds->n);
+    p->caps.ids_cap[0] = ids0;
+    p->caps.ids_cap[1] = ids1;
+    SKC_TRY(plan_pipeline(p, Arena::RECORD, s));
+    SKC_CUDA(cudaStreamSynchronize(s));
+    if (plan_fits(p)) break;
+    if (tries == 3) return set_error(SKC_ERR_INVALID, "plan capacities do not settle");
+    // A clamped candidate count also clamped the totals: grow them more.
+    const bool m_over = p->h_stats[0] > p->caps.m_cap;
+    m_cap = std::max(m_cap, with_slack(p->h_stats[0]));
+    ids0 = std::max(ids0 * (m_over ? 2 : 1), with_slack(p->h_stats[1]));
+    ids1 = std::max(ids1 * (m_over ? 2 : 1), with_slack(p->h_stats[2]));
+  }
+  t_capturing = true;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
+  int st = e == cudaSuccess
+               ? plan_pipeline(p, Arena::REPLAY, s)
+               : set_error(SKC_ERR_CUDA, "stream capture failed: %s", cudaGetErrorString(e));
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(s, &g) : cudaSuccess;
+  t_capturing = false;
+  if (st != SKC_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e2 != cudaSuccess || !g)
+    return set_error(SKC_ERR_CUDA, "stream capture failed: %s", cudaGetErrorString(e2));
+  p->graph = g;
+  SKC_CUDA(cudaGraphInstantiate(&p->exec, g, 0));
+  size_t nn = 0;
+  SKC_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+  std::vector<cudaGraphNode_t> nodes(nn);
+  SKC_CUDA(cudaGraphGetNodes(g, nodes.data(), &nn));
+  p->kernels = 0;
+  for (cudaGraphNode_t node : nodes) {
+    cudaGraphNodeType t;
+    SKC_CUDA(cudaGraphNodeGetType(node, &t));
+    if (t == cudaGraphNodeTypeKernel) ++p->kernels;
+  }
+  return SKC_OK;
+}
+
+// Device copy of a plan output into memory the result owns.
+template <typename T>
+static int copy_out(cudaStream_t s, const T* src, uint64_t count, T** dst) {
+  *dst = nullptr;
+  if (!src) return SKC_OK;
+  SKC_CUDA(cudaMallocAsync((void**)dst, std::max<uint64_t>(count, 1) * sizeof(T), s));
+  if (count) SKC_CUDA(cudaMemcpyAsync(*dst, src, count * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  return SKC_OK;
+}
+
+extern "C" {
+
+int skc_plan_create(skc_context* ctx, skc_dataset* ds, const skc_options* opt, skc_plan** out) {
+  clear_error();
+  if (!ctx || !ds || !out) return set_error(SKC_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (ds->ctx != ctx) return set_error(SKC_ERR_INVALID, "dataset belongs to another (or a destroyed) context");
+  skc_options o;
+  SKC_TRY(check_options(ds, opt, &o));
+  if (o.mode != SKC_MODE_BATCHED || o.subspace)
+    return set_error(SKC_ERR_UNSUPPORTED, "plans capture the BATCHED skycube only");
+  SKC_CUDA(cudaSetDevice(ctx->device));
+  auto* p = new skc_plan;
+  p->ctx = ctx;
+  p->ds = ds;
+  p->opt = o;
+  p->max_d = (o.max_d <= 0 || o.max_d > ds->d) ? ds->d : o.max_d;
+  int st = resolve_params(ds, ctx->stream, o, p->max_d, &p->P);
+  // One ordinary run gives the sizes the capacities start from.
+  skc_result* R = nullptr;
+  if (st == SKC_OK) {
+    Exec E;
+    E.ctx = ctx;
+    E.stream = ctx->stream;
+    st = skycube_exec(E, ds, &o, &R, &p->P);
+  }
+  if (st == SKC_OK && cudaMallocHost(&p->h_stats, 4 * sizeof(uint64_t)) != cudaSuccess)
+    st = set_error(SKC_ERR_OOM, "pinned host allocation failed");
+  if (st == SKC_OK) {
+    {
+      std::lock_guard<std::mutex> lock(ctx->mu);
+      ctx->plans.insert(p);
+    }
+    st = plan_build(p, with_slack(R->n_cand), with_slack(R->total_ids), with_slack(R->total_ext));
+  }
+  if (R) skc_result_free(R);
+  if (st != SKC_OK) {
+    std::string msg = g_err;
+    release_plan_memory(p);
+    if (p->h_stats) cudaFreeHost(p->h_stats);
+    delete p;
+    g_err = msg;
+    return st;
+  }
+  *out = p;
+  return SKC_OK;
+}
+
+int skc_plan_execute(skc_plan* p, skc_result** out) {
+  clear_error();
+  if (!p) return set_error(SKC_ERR_INVALID, "NULL plan");
+  if (out) *out = nullptr;
+  if (!p->ctx) return set_error(SKC_ERR_INVALID, "plan's context was destroyed");
+  if (!p->ds) return set_error(SKC_ERR_INVALID, "plan's dataset was freed");
+  skc_context* ctx = p->ctx;
+  cudaStream_t s = ctx->stream;
+  SKC_CUDA(cudaSetDevice(ctx->device));
+  for (int attempt = 0;; ++attempt) {
+    SKC_CUDA(cudaEventRecord(ctx->ev_start, s));
+    SKC_CUDA(cudaGraphLaunch(p->exec, s));
+    SKC_CUDA(cudaEventRecord(ctx->ev_stop, s));
+    g_launches.fetch_add(p->kernels, std::memory_order_relaxed);
+    SKC_CUDA(cudaStreamSynchronize(s));
+    if (plan_fits(p)) break;
+    if (attempt == 1) return set_error(SKC_ERR_INVALID, "plan capacities do not settle");
+    // The points changed (skc_dataset_update): re-size and capture again.
+    ++p->replans;
+    const bool m_over = p->h_stats[0] > p->caps.m_cap;
+    SKC_TRY(plan_build(p, std::max(p->caps.m_cap, with_slack(p->h_stats[0])),
+                       std::max(p->caps.ids_cap[0] * (m_over ? 2 : 1), with_slack(p->h_stats[1])),
+                       std::max(p->caps.ids_cap[1] * (m_over ? 2 : 1), with_slack(p->h_stats[2]))));
+  }
+  float ms = 0.f;
+  SKC_CUDA(cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop));
+  ctx->last_ms = ms;
+  ctx->phases.assign(1, {std::string("plan graph"), ms});
+  if (!out) return SKC_OK;
+  const uint64_t m = p->h_stats[0];
+  const uint32_t nsub = 1u << p->ds->d;
+  auto* R = new skc_result;
+  R->ctx = ctx;
+  R->stream = s;
+  R->d = p->outs.d;
+  R->max_d = p->outs.max_d;
+  R->algo = p->outs.algo;
+  R->n_cand = m;
+  R->total_ids = p->h_stats[1];
+  R->total_ext = p->outs.d_eids ? p->h_stats[2] : 0;
+  R->words = p->outs.words;
+  int st = copy_out(s, p->outs.d_off, nsub + 1, &R->d_off);
+  if (st == SKC_OK) st = copy_out(s, p->outs.d_ids, R->total_ids, &R->d_ids);
+  if (st == SKC_OK) st = copy_out(s, p->outs.d_eoff, nsub + 1, &R->d_eoff);
+  if (st == SKC_OK) st = copy_out(s, p->outs.d_eids, R->total_ext, &R->d_eids);
+  if (st == SKC_OK) st = copy_out(s, p->outs.d_bits, m * p->outs.words, &R->d_bits);
+  if (st == SKC_OK) st = copy_out(s, p->outs.d_cand, m, &R->d_cand);
+  if (st == SKC_OK && cudaStreamSynchronize(s) != cudaSuccess)
+    st = set_error(SKC_ERR_CUDA, "plan result copy failed");
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->results.insert(R);
+  }
+  if (st != SKC_OK) {
+    std::string msg = g_err;
+    skc_result_free(R);
+    g_err = msg;
+    return st;
+  }
+  *out = R;
+  return SKC_OK;
+}
+
+int skc_plan_info(skc_plan* p, uint64_t* kernels, uint64_t* replans, uint64_t* cand_capacity,
+                  uint64_t* ids_capacity) {
+  clear_error();
+  if (!p) return set_error(SKC_ERR_INVALID, "NULL plan");
+  if (kernels) *kernels = p->kernels;
+  if (replans) *replans = p->replans;
+  if (cand_capacity) *cand_capacity = p->caps.m_cap;
+  if (ids_capacity) *ids_capacity = p->caps.ids_cap[0];
+  return SKC_OK;
+}
+
+int skc_plan_destroy(skc_plan* p) {
+  if (!p) return SKC_OK;
+  if (p->ctx) {
+    cudaSetDevice(p->ctx->device);
+    cudaStreamSynchronize(p->ctx->stream);
+    release_plan_memory(p);
+  }
+  delete p;
+  return SKC_OK;
+}
+
+int skc_dataset_update(skc_dataset* ds, const float* rows) {
+  clear_error();
+  if (!ds || !rows) return set_error(SKC_ERR_INVALID, "NULL argument");
+  skc_context* ctx = ds->ctx;
+  if (!ctx) return set_error(SKC_ERR_INVALID, "dataset's context was destroyed");
+  SKC_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const uint64_t n = ds->n;
+  const int d = ds->d;
+  uint32_t h_bad = 0;
+  {
+    Arena A(s);
+    float *tmp, *soa;
+    uint32_t* bad;
+    SKC_TRY(A.alloc(&tmp, n * d));
+    SKC_TRY(A.alloc(&soa, (uint64_t)d * ds->n_pad));
+    SKC_TRY(A.alloc(&bad, 1));
+    SKC_CUDA(cudaMemcpyAsync(tmp, rows, n * d * sizeof(float), cudaMemcpyHostToDevice, s));
+    SKC_CUDA(cudaMemsetAsync(bad, 0, sizeof(uint32_t), s));
+    SKC_TRY(launch_rows_to_soa(s, tmp, n, d, ds->n_pad, soa, bad));
+    SKC_CUDA(cudaMemcpyAsync(&h_bad, bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    SKC_CUDA(cudaStreamSynchronize(s));
+    if (!h_bad) {
+      // The dataset may live on another stream: order the copy after it.
+      if (ds->stream && ds->stream != s) SKC_CUDA(cudaStreamSynchronize(ds->stream));
+      SKC_CUDA(cudaMemcpyAsync(ds->x, soa, (size_t)d * ds->n_pad * sizeof(float),
+                               cudaMemcpyDeviceToDevice, s));
+      SKC_CUDA(cudaStreamSynchronize(s));
+    }
+  }
+  if (h_bad) return set_error(SKC_ERR_INVALID, "%u non-finite attribute values (NaN/inf) rejected", h_bad);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ds->sig_ready = false;
+  return SKC_OK;
+}
+
+int skc_autotune(skc_context* ctx, skc_dataset* ds, const skc_options* base, int repeats,
+                 skc_options* best, float* best_ms) {
+  clear_error();
+  if (!ctx || !ds) return set_error(SKC_ERR_INVALID, "NULL argument");
+  if (ds->ctx != ctx) return set_error(SKC_ERR_INVALID, "dataset belongs to another (or a destroyed) context");
+  skc_options o;
+  SKC_TRY(check_options(ds, base, &o));
+  if (repeats <= 0) repeats = 2;
+  if (repeats > 16) repeats = 16;
+  const int d = ds->d;
+  const int max_d = (o.max_d <= 0 || o.max_d > d) ? d : o.max_d;
+  const uint64_t n = ds->n;
+  Exec E;
+  E.ctx = ctx;
+  E.stream = ctx->stream;
+  SKC_CUDA(cudaSetDevice(ctx->device));
+  uint32_t sig[3];
+  SKC_TRY(dataset_signature(ds, E.stream, sig));
+
+  // Start from the explicit options and the defaults (not from the table).
+  RunParams cur;
+  cur.depth = o.depth ? o.depth : auto_depth(n, d);
+  const int pq0 = o.pq_size > 0 ? o.pq_size
+                  : o.pq_size < 0 ? 0
+                                  : (n >= kPrefilterMinPoints ? kDefaultPruners : 0);
+  cur.pq_size = (pq0 > 0 && n > 2ull * (uint64_t)pq0) ? pq0 : 0;
+  cur.tile_points = o.tile_points ? o.tile_points : kDefaultTilePoints;
+  cur.chunk = o.chunk ? o.chunk : 1;
+  cur.blocks_per_sm = o.blocks_per_sm;
+
+  auto time_run = [&](const RunParams& P, float* ms) -> int {
+    float bestv = 3.0e38f;
+    for (int r = 0; r < repeats; ++r) {
+      skc_result* R = nullptr;
+      SKC_TRY(skycube_exec(E, ds, &o, &R, &P));
+      bestv = std::min(bestv, E.ms);
+      skc_result_free(R);
+    }
+    *ms = bestv;
+    return SKC_OK;
+  };
+  float cur_ms = 0.f;
+  SKC_TRY(time_run(cur, &cur_ms));
+
+  // One pass of coordinate search over the parameters the options leave
+  // automatic; a change is kept when it is at least 2% faster.
+  const bool bitmap_stage = !o.subspace && !(o.algo == SKC_ALGO_SDSC && o.mode == SKC_MODE_PLAIN);
+  auto try_values = [&](int RunParams::*field, const std::vector<int>& values) -> int {
+    for (int v : values) {
+      if (cur.*field == v) continue;
+      RunParams P = cur;
+      P.*field = v;
+      float ms = 0.f;
+      SKC_TRY(time_run(P, &ms));
+      if (ms < 0.98f * cur_ms) {
+        cur = P;
+        cur_ms = ms;
+      }
+    }
+    return SKC_OK;
+  };
+  if (!o.depth) SKC_TRY(try_values(&RunParams::depth, {7, 6, 5, 4, 3}));
+  if (!o.pq_size) {
+    std::vector<int> pqs;
+    for (int v : {0, 32, 128, 512})
+      if (v == 0 || n > 2ull * (uint64_t)v) pqs.push_back(v);
+    SKC_TRY(try_values(&RunParams::pq_size, pqs));
+  }
+  if (bitmap_stage) {
+    if (!o.tile_points) SKC_TRY(try_values(&RunParams::tile_points, {64, 256, 1024}));
+    if (!o.chunk) SKC_TRY(try_values(&RunParams::chunk, {1, 4, 16}));
+    if (!o.blocks_per_sm) SKC_TRY(try_values(&RunParams::blocks_per_sm, {0, 1, 2}));
+  }
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    ctx->tunings[tuning_key(ds, sig, o, max_d)] =
+        skc_context::Tuned{cur.depth, cur.pq_size, cur.tile_points, cur.chunk, cur.blocks_per_sm,
+                           cur_ms};
+  }
+  if (best) {
+    *best = o;
+    best->depth = cur.depth;
+    best->pq_size = cur.pq_size > 0 ? cur.pq_size : -1;
+    best->tile_points = cur.tile_points;
+    best->chunk = cur.chunk;
+    best->blocks_per_sm = cur.blocks_per_sm;
+  }
+  if (best_ms) *best_ms = cur_ms;
+  ctx->phases = E.phases;
+  ctx->last_ms = E.ms;
+  return SKC_OK;
+}
+
+int skc_dataset_signature(skc_dataset* ds, int* size_class, int* sky_class, int* ties) {
+  clear_error();
+  if (!ds) return set_error(SKC_ERR_INVALID, "NULL dataset");
+  if (!ds->ctx) return set_error(SKC_ERR_INVALID, "dataset's context was destroyed");
+  SKC_CUDA(cudaSetDevice(ds->ctx->device));
+  uint32_t sig[3];
+  SKC_TRY(dataset_signature(ds, ds->ctx->stream, sig));
+  int sc, kc, t;
+  signature_classes(ds, sig, &sc, &kc, &t);
+  if (size_class) *size_class = sc;
+  if (sky_class) *sky_class = kc;
+  if (ties) *ties = t;
+  return SKC_OK;
+}
+
+int skc_tuning_count(skc_context* ctx, uint64_t* count) {
+  clear_error();
+  if (!ctx || !count) return set_error(SKC_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  *count = ctx->tunings.size();
+  return SKC_OK;
+}
+
+int skc_tuning_clear(skc_context* ctx) {
+  clear_error();
+  if (!ctx) return set_error(SKC_ERR_INVALID, "NULL context");
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->tunings.clear();
+  return SKC_OK;
 }
 
 int skc_result_info(skc_result* r, int* d, uint64_t* n_cand, uint64_t* total) {

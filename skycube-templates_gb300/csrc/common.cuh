@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <mutex>
 #include <set>
 #include <string>
@@ -95,8 +96,15 @@ struct skc_context {
   // their device memory and detaches them (ctx = nullptr).
   std::set<skc_dataset*> datasets;
   std::set<skc_result*> results;
+  std::set<skc_plan*> plans;
   // Per-phase device times of the last skc_skycube.
   std::vector<std::pair<std::string, float>> phases;
+  // Work parameters chosen by skc_autotune, by signature key (api.cu).
+  struct Tuned {
+    int depth, pq_size, tile_points, chunk, blocks_per_sm;
+    float ms;
+  };
+  std::map<uint64_t, Tuned> tunings;
   // Guards the table caches and the object registries (the serving loop
   // runs pipelines from several host threads).
   std::mutex mu;
@@ -109,6 +117,11 @@ struct skc_dataset {
   uint64_t n_pad = 0;  // n rounded up to a multiple of 128
   int d = 0;
   float* x = nullptr;  // attribute-major (SoA): x[k * n_pad + i]
+  // Distribution signature from a point sample, computed on first use
+  // (guarded by the context's mutex): sample size, sample points on the
+  // sample's own skyline, sample points sharing a value with another.
+  bool sig_ready = false;
+  uint32_t sig_samples = 0, sig_sky = 0, sig_tied = 0;
 };
 
 struct skc_result {

@@ -53,6 +53,10 @@ int launch_merge_disjoint(cudaStream_t s, const uint32_t* a, uint32_t na,
                           const uint32_t* b, uint32_t nb, uint32_t* out);
 int launch_gather_u32(cudaStream_t s, const uint32_t* in, const uint32_t* perm,
                       const uint32_t* m_ptr, uint64_t m_max, uint32_t* out);
+int launch_sample_signature(cudaStream_t s, const float* x, uint64_t n_pad, uint64_t n, int d,
+                            uint32_t* out);
+int launch_cap_count(cudaStream_t s, uint32_t* m_ptr, uint32_t cap, uint64_t* stats, int slot);
+int launch_stat_u64(cudaStream_t s, const uint64_t* src, uint64_t* stats, int slot);
 int launch_csr_assemble(cudaStream_t s, const uint32_t* src,
                         const uint64_t* src_off, const uint64_t* dst_off,
                         uint32_t ncub, uint32_t* dst);
@@ -123,6 +127,36 @@ int launch_partition_skyline(cudaStream_t s, int d, int depth,
                              const LevelTables& T, const PartitionSkylineArgs& a,
                              const PartScratch& ps);
 
+// prefilter.cu: pruner prefilter of a list on subspace S. Survivors (the
+// entries no pruner strictly dominates) come out as point ids in list order.
+constexpr int kMaxPruners = 1024;
+struct PrefilterScratch {
+  uint32_t* hist;      // [prefilter_sum_bins()]
+  uint32_t* sel;       // [8]
+  uint32_t* pr_ids;    // [K]
+  uint32_t* pr_key;    // [K]
+  uint4* pr_cells;     // [K] pruner cells, rank order
+  float* pr_x;         // [d * K] pruner floats, rank order
+  uint8_t* st;         // [m_max]
+  uint32_t* blk0;      // [m_max / 1024 + 1]
+  uint32_t* blk1;      // [m_max / 1024 + 1]
+};
+struct PrefilterArgs {
+  const uint4* cells;    // point id -> grid cells
+  const float* x;        // attribute-major points, pitch n_pad
+  uint64_t n_pad;
+  const uint32_t* ids;   // list position -> point id (nullptr: identity)
+  const uint32_t* m_ptr;
+  uint64_t m_max;
+  uint32_t S;
+  uint32_t K;            // pruners, 1 .. kMaxPruners
+  PrefilterScratch ps;
+};
+int launch_prefilter(cudaStream_t s, int d, int num_sms, const PrefilterArgs& a,
+                     uint32_t* out_ids, uint32_t* out_count);
+uint32_t prefilter_sum_bins();
+size_t prefilter_smem(int d, uint32_t K);
+
 // mdmc.cu: per-point dominated-subspace bitmaps over the candidate set.
 struct BitmapArgs {
   const uint4* pcells;   // candidate order
@@ -138,6 +172,7 @@ struct BitmapArgs {
   int depth;
   const uint32_t* m_ptr;
   uint32_t* work;        // work counter, must hold p_begin
+  uint32_t chunk;        // candidates per work-counter grab (0: 1)
   uint32_t p_end;        // stop at min(m, p_end)
   uint32_t* out_dom;     // [m][words] dominated bitmaps
   uint32_t* out_ext;     // [m][words] extended-skyline bitmaps, or nullptr
@@ -161,6 +196,7 @@ struct CompactArgs {
   uint64_t* bsum;        // scan scratch
   uint64_t* csr_off;     // [nsub + 1] output offsets per cuboid
   uint32_t* out;         // ids (sized by the caller after the count pass)
+  uint64_t out_cap;      // entries of `out`; ids past it are not written
 };
 uint32_t compact_tiles(uint64_t m_max);
 int launch_bits_count(cudaStream_t s, const CompactArgs& a);

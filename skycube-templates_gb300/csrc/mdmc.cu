@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(256) k_bitmaps(
     const float* __restrict__ qx, const uint4* __restrict__ bmin,
     const uint32_t* __restrict__ boff, const uint32_t* __restrict__ unrank,
     uint32_t K, int B, int depth,
-    const uint32_t* __restrict__ m_ptr, uint32_t* __restrict__ work,
+    const uint32_t* __restrict__ m_ptr, uint32_t* __restrict__ work, uint32_t chunk,
     uint32_t p_end_cap, uint32_t* __restrict__ out_dom,
     uint32_t* __restrict__ out_ext, uint32_t* __restrict__ tie_slab) {
   using BS = BitState<D>;
@@ -158,11 +158,13 @@ __global__ void __launch_bounds__(256) k_bitmaps(
   const int sh = depth - 1;
 
   for (;;) {
-    uint32_t p = 0;
-    if (lane == 0) p = atomicAdd(work, 1u);
-    p = __shfl_sync(kFull, p, 0);
-    if (p >= pend) break;
-
+    // The warp takes `chunk` consecutive candidates per grab.
+    uint32_t p0 = 0;
+    if (lane == 0) p0 = atomicAdd(work, chunk);
+    p0 = __shfl_sync(kFull, p0, 0);
+    if (p0 >= pend) break;
+    const uint32_t p1 = min(pend, p0 + chunk);
+    for (uint32_t p = p0; p < p1; ++p) {
     const uint4 pc4 = pcells[p];
     uint32_t pc[NW], pH[NW];
 #pragma unroll
@@ -351,6 +353,7 @@ __global__ void __launch_bounds__(256) k_bitmaps(
       }
     }
     __syncwarp();
+    }
   }
 }
 
@@ -377,7 +380,8 @@ static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
   if (a.grid_blocks > 0 && a.grid_blocks < grid) grid = a.grid_blocks;
   k_bitmaps<D><<<grid, 256, smem, s>>>(a.pcells, a.px, a.p_pad, a.qcells, a.qx,
                                         a.bmin, a.boff, a.unrank, a.K, a.B, a.depth,
-                                        a.m_ptr, a.work, a.p_end, a.out_dom, a.out_ext,
+                                        a.m_ptr, a.work, a.chunk ? a.chunk : 1u, a.p_end,
+                                        a.out_dom, a.out_ext,
                                         a.tie_slab);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
@@ -487,7 +491,7 @@ __global__ void __launch_bounds__(256) k_bits_write(
     const uint32_t* __restrict__ bits, uint32_t W,
     const uint32_t* __restrict__ m_ptr, uint32_t T, int count_set,
     uint32_t nsub, int max_d, const uint64_t* __restrict__ offs,
-    const uint32_t* __restrict__ cand, uint32_t* __restrict__ out) {
+    const uint32_t* __restrict__ cand, uint32_t* __restrict__ out, uint64_t out_cap) {
   __shared__ uint32_t wc[8][32];
   __shared__ uint32_t run[8][32];
   const uint32_t t = blockIdx.x, w = blockIdx.y;
@@ -530,8 +534,10 @@ __global__ void __launch_bounds__(256) k_bits_write(
       const uint32_t c = w * 32 + b;
       if (!cuboid_wanted(c, nsub, max_d)) continue;
       const uint32_t base = run[k][b];
-      if ((v >> b) & 1u)
-        out[offs[(uint64_t)c * T + t] + base + __popc(bal & lt_mask)] = id;
+      if ((v >> b) & 1u) {
+        const uint64_t pos = offs[(uint64_t)c * T + t] + base + __popc(bal & lt_mask);
+        if (pos < out_cap) out[pos] = id;
+      }
       __syncwarp();
       if (lane == 0) run[k][b] = base + __popc(bal);
       __syncwarp();
@@ -562,7 +568,8 @@ int launch_bits_count(cudaStream_t s, const CompactArgs& a) {
 int launch_bits_write(cudaStream_t s, const CompactArgs& a) {
   const uint32_t T = compact_tiles(a.m_max);
   k_bits_write<<<dim3(T, a.words), 256, 0, s>>>(a.bits, a.words, a.m_ptr, T, a.count_set,
-                                                 a.nsub, a.max_d, a.offs, a.cand, a.out);
+                                                 a.nsub, a.max_d, a.offs, a.cand, a.out,
+                                                 a.out_cap);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }

@@ -640,4 +640,83 @@ int launch_gather_u32(cudaStream_t s, const uint32_t* in, const uint32_t* perm,
   return SKC_OK;
 }
 
+// Distribution signature of a dataset from a strided sample of up to
+// kSignatureSamples points: out[0] = sample points on the sample's own
+// full-space skyline, out[1] = sample points that share an attribute value
+// with another sample point, out[2] = sample size. It keys the autotuner's
+// table (correlated, independent and anticorrelated data differ by orders
+// of magnitude in the first; tie-heavy data shows in the second).
+constexpr uint32_t kSignatureSamples = 512;
+
+__global__ void __launch_bounds__(kSignatureSamples) k_sample_signature(
+    const float* __restrict__ x, uint64_t n_pad, uint64_t n, int d,
+    uint32_t* __restrict__ out) {
+  __shared__ float xs[kMaxDims][kSignatureSamples];
+  __shared__ uint32_t cnt[2];
+  const uint32_t ns = (uint32_t)(n < kSignatureSamples ? n : kSignatureSamples);
+  const uint32_t t = threadIdx.x;
+  if (t < 2) cnt[t] = 0;
+  if (t < ns) {
+    const uint64_t id = (uint64_t)t * n / ns;
+    for (int k = 0; k < d; ++k) xs[k][t] = x[(uint64_t)k * n_pad + id];
+  }
+  __syncthreads();
+  if (t < ns) {
+    bool dominated = false, tied = false;
+    for (uint32_t j = 0; j < ns; ++j) {
+      if (j == t) continue;
+      bool le = true, lt = false;
+      for (int k = 0; k < d; ++k) {
+        const float a = xs[k][j], b = xs[k][t];
+        le &= a <= b;
+        lt |= a < b;
+        tied |= a == b;
+      }
+      dominated |= le && lt;
+    }
+    if (!dominated) atomicAdd(&cnt[0], 1u);
+    if (tied) atomicAdd(&cnt[1], 1u);
+  }
+  __syncthreads();
+  if (t == 0) {
+    out[0] = cnt[0];
+    out[1] = cnt[1];
+    out[2] = ns;
+  }
+}
+
+int launch_sample_signature(cudaStream_t s, const float* x, uint64_t n_pad, uint64_t n, int d,
+                            uint32_t* out) {
+  if (d < 1 || d > kMaxDims) return set_error(SKC_ERR_INVALID, "unsupported d=%d", d);
+  k_sample_signature<<<1, kSignatureSamples, 0, s>>>(x, n_pad, n, d, out);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
+// Plan helpers (graph-captured launch sequences, api.cu). k_cap_count
+// records the true list length in stats[slot] and clamps the device count to
+// the plan's capacity, so every later kernel stays inside the buffers; the
+// host sees the overflow and re-plans. k_stat_u64 copies one device total.
+__global__ void k_cap_count(uint32_t* m_ptr, uint32_t cap, uint64_t* stats, int slot) {
+  const uint32_t m = *m_ptr;
+  stats[slot] = m;
+  if (m > cap) *m_ptr = cap;
+}
+
+__global__ void k_stat_u64(const uint64_t* src, uint64_t* stats, int slot) {
+  stats[slot] = *src;
+}
+
+int launch_cap_count(cudaStream_t s, uint32_t* m_ptr, uint32_t cap, uint64_t* stats, int slot) {
+  k_cap_count<<<1, 1, 0, s>>>(m_ptr, cap, stats, slot);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
+int launch_stat_u64(cudaStream_t s, const uint64_t* src, uint64_t* stats, int slot) {
+  k_stat_u64<<<1, 1, 0, s>>>(src, stats, slot);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
 }  // namespace skc

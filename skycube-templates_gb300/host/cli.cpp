@@ -16,7 +16,9 @@
 // (src/main.h:72-110); this driver compares full id sets per cuboid against
 // the engine's other, independent algorithm (the per-cuboid skyline for
 // -s mdmc, the bitmap form for -s sdsc) and exits 1 on any difference.
-// -t, -a, -q and -p are accepted for compatibility (no CPU workers run).
+// -q sets the prefilter's pruner count for mdmc (the suite's pq_size, capped
+// at 1024). -t, -a and -p are accepted for compatibility (no CPU workers
+// run).
 #include <getopt.h>
 
 #include <chrono>
@@ -41,7 +43,8 @@ void usage() {
   printf(" -e: execution form: batched (one launch for all cuboids, default) | plain\n");
   printf(" -c: check the result against the engine's other algorithm (id sets)\n");
   printf(" -o: print the work distribution\n");
-  printf(" -p, -t, -a, -q, -i: accepted for compatibility; no CPU workers run\n\n");
+  printf(" -q: prefilter pruners for mdmc (default 128, at most 1024)\n");
+  printf(" -p, -t, -a, -i: accepted for compatibility; no CPU workers run\n\n");
 }
 
 std::vector<float> split_line(const std::string& line, bool* ok) {

@@ -247,6 +247,8 @@ class MDMC {
     o.mode = skc::mode_of(cfg_);
     o.max_d = cfg_ ? cfg_->max_d : 0;
     o.depth = cfg_ ? (int)cfg_->partitioning_depth : 0;
+    // The suite's MDMC prefilters with pq_size pruners (src/mdmc/MDMC.cu:251).
+    o.pq_size = cfg_ ? (int)std::min<uint32_t>(cfg_->pq_size, 1024) : 0;
     o.want_bitmaps = 1;
     if (res_) skc_result_free(res_);
     res_ = nullptr;

@@ -41,7 +41,13 @@ class _Timing(ctypes.Structure):
 class _Options(ctypes.Structure):
     _fields_ = [("algo", ctypes.c_int), ("mode", ctypes.c_int), ("max_d", ctypes.c_int),
                 ("depth", ctypes.c_int), ("want_extended", ctypes.c_int),
-                ("want_bitmaps", ctypes.c_int), ("subspace", ctypes.c_uint32)]
+                ("want_bitmaps", ctypes.c_int), ("subspace", ctypes.c_uint32),
+                ("pq_size", ctypes.c_int), ("tile_points", ctypes.c_int),
+                ("chunk", ctypes.c_int), ("blocks_per_sm", ctypes.c_int)]
+
+    def work_params(self):
+        return {"depth": self.depth, "pq_size": self.pq_size, "tile_points": self.tile_points,
+                "chunk": self.chunk, "blocks_per_sm": self.blocks_per_sm}
 
 
 _lib = None
@@ -82,6 +88,15 @@ def lib():
         "skc_server_wait": (i32, [vp, u64, P(vp), P(_Timing)]),
         "skc_server_stats": (i32, [vp, P(u64), P(u64), P(u64)]),
         "skc_server_destroy": (i32, [vp]),
+        "skc_autotune": (i32, [vp, vp, P(_Options), i32, P(_Options), P(ctypes.c_float)]),
+        "skc_dataset_signature": (i32, [vp, P(i32), P(i32), P(i32)]),
+        "skc_tuning_count": (i32, [vp, P(u64)]),
+        "skc_tuning_clear": (i32, [vp]),
+        "skc_plan_create": (i32, [vp, vp, P(_Options), P(vp)]),
+        "skc_plan_execute": (i32, [vp, P(vp)]),
+        "skc_plan_info": (i32, [vp, P(u64), P(u64), P(u64), P(u64)]),
+        "skc_plan_destroy": (i32, [vp]),
+        "skc_dataset_update": (i32, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -136,6 +151,14 @@ class Context:
         _check(lib().skc_last_device_ms(self.handle, ctypes.byref(v)))
         return v.value
 
+    def tuning_count(self):
+        v = ctypes.c_uint64()
+        _check(lib().skc_tuning_count(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def tuning_clear(self):
+        _check(lib().skc_tuning_clear(self.handle))
+
 
 class Dataset:
     """A point set resident on the device (MDMC<D>::Init / SDSC<D>::Init)."""
@@ -156,6 +179,13 @@ class Dataset:
                                             self.n, self.d, ctypes.byref(h)))
         self.handle = h
         ctx._adopt(self)
+
+    def update(self, points):
+        """skc_dataset_update: new points in place (same n and d)."""
+        x = np.ascontiguousarray(points, dtype=np.float32)
+        if x.shape != (self.n, self.d):
+            raise SkycubeError(1, f"update needs shape {(self.n, self.d)}, got {x.shape}")
+        _check(lib().skc_dataset_update(self.handle, x.ctypes.data_as(ctypes.c_void_p)))
 
     def close(self):
         if self.handle:
@@ -247,20 +277,84 @@ def kernel_launches():
 
 
 def options(algo="mdmc", mode="batched", max_d=0, depth=0, want_extended=False,
-            want_bitmaps=False, subspace=0):
+            want_bitmaps=False, subspace=0, pq_size=0, tile_points=0, chunk=0,
+            blocks_per_sm=0):
+    """skc_options. The work parameters (depth, pq_size, tile_points, chunk,
+    blocks_per_sm) change the work, never the result; 0 = automatic (a stored
+    tuning for datasets like this one, else the default); pq_size < 0 turns
+    the prefilter off."""
     return _Options(ALGOS[algo], MODES[mode], int(max_d), int(depth),
-                    int(bool(want_extended)), int(bool(want_bitmaps)), int(subspace))
+                    int(bool(want_extended)), int(bool(want_bitmaps)), int(subspace),
+                    int(pq_size), int(tile_points), int(chunk), int(blocks_per_sm))
 
 
 def skycube(ctx, ds, algo="mdmc", mode="batched", max_d=0, depth=0,
-            want_extended=False, want_bitmaps=False, subspace=0):
+            want_extended=False, want_bitmaps=False, subspace=0, pq_size=0,
+            tile_points=0, chunk=0, blocks_per_sm=0):
     """Computes the skycube of a resident dataset (MDMC/SDSC ::Execute), or
     with `subspace` set, only that cuboid's skyline (a skyline query)."""
-    o = options(algo, mode, max_d, depth, want_extended, want_bitmaps, subspace)
+    o = options(algo, mode, max_d, depth, want_extended, want_bitmaps, subspace, pq_size,
+                tile_points, chunk, blocks_per_sm)
     h = ctypes.c_void_p()
     _check(lib().skc_skycube(ctx.handle, ds.handle, ctypes.byref(o), ctypes.byref(h)))
     md = ds.d if max_d <= 0 or max_d > ds.d else max_d
     return Result(ctx, h, ds.d, md)
+
+
+class Plan:
+    """skc_plan_*: the batched skycube of one dataset captured as a CUDA
+    graph; execute() replays it on the dataset's current points."""
+
+    def __init__(self, ctx, ds, **opts):
+        self.ctx, self.ds = ctx, ds
+        o = options(**opts)
+        self.max_d = ds.d if o.max_d <= 0 or o.max_d > ds.d else o.max_d
+        h = ctypes.c_void_p()
+        _check(lib().skc_plan_create(ctx.handle, ds.handle, ctypes.byref(o), ctypes.byref(h)))
+        self.handle = h
+        ctx._adopt(self)
+
+    def execute(self):
+        h = ctypes.c_void_p()
+        _check(lib().skc_plan_execute(self.handle, ctypes.byref(h)))
+        return Result(self.ctx, h, self.ds.d, self.max_d)
+
+    def info(self):
+        k, r, c, i = (ctypes.c_uint64() for _ in range(4))
+        _check(lib().skc_plan_info(self.handle, ctypes.byref(k), ctypes.byref(r), ctypes.byref(c),
+                                   ctypes.byref(i)))
+        return {"kernels": k.value, "replans": r.value, "cand_capacity": c.value,
+                "ids_capacity": i.value}
+
+    def close(self):
+        if self.handle:
+            lib().skc_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune(ctx, ds, repeats=2, **opts):
+    """skc_autotune: times the work parameters left at 0 in `opts` on `ds`,
+    stores the winner for datasets with the same signature and returns
+    (chosen work parameters as a dict, device ms)."""
+    base = options(**opts)
+    best = _Options()
+    ms = ctypes.c_float()
+    _check(lib().skc_autotune(ctx.handle, ds.handle, ctypes.byref(base), int(repeats),
+                              ctypes.byref(best), ctypes.byref(ms)))
+    return best.work_params(), ms.value
+
+
+def signature(ds):
+    """skc_dataset_signature: {size_class, sky_class, ties}."""
+    a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _check(lib().skc_dataset_signature(ds.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+    return {"size_class": a.value, "sky_class": b.value, "ties": c.value}
 
 
 class Server:

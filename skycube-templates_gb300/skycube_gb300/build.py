@@ -22,7 +22,8 @@ LIB_PATH = os.path.join(BUILD, LIB_NAME)
 CLI_PATH = os.path.join(BUILD, "skycube")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["api.cu", "prep.cu", "skyline.cu", "partition.cu", "mdmc.cu", "noalloc.cu"]
+CU_SOURCES = ["api.cu", "prep.cu", "skyline.cu", "partition.cu", "mdmc.cu", "noalloc.cu",
+              "prefilter.cu"]
 
 
 def _nvcc():

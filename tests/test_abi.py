@@ -44,8 +44,25 @@ def test_library_exports_every_declared_symbol(built):
 
 def test_options_defaults(built):
     o = sk._Options()
+    o.pq_size = o.chunk = 9
     sk.lib().skc_options_init(ctypes.byref(o))
     assert (o.algo, o.mode, o.max_d, o.depth) == (0, 1, 0, 0)
+    assert (o.pq_size, o.tile_points, o.chunk, o.blocks_per_sm) == (0, 0, 0, 0)
+
+
+def test_options_layout_matches_header(tmp_path):
+    """The ctypes mirror of skc_options has the C struct's size and offsets."""
+    src = tmp_path / "layout.c"
+    fields = [f for f, _ in sk._Options._fields_]
+    body = "".join(f'printf("%zu ", offsetof(skc_options, {f}));' for f in fields)
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "skycube_gb300.h"\n'
+                   f'int main(void) {{ printf("%zu ", sizeof(skc_options)); {body} return 0; }}\n')
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    want = [ctypes.sizeof(sk._Options)] + [getattr(sk._Options, f).offset for f in fields]
+    assert got == want
 
 
 def test_null_arguments_are_rejected(built):
@@ -53,6 +70,14 @@ def test_null_arguments_are_rejected(built):
     assert L.skc_context_create(0, None) == 1
     assert L.skc_skycube(None, None, None, None) == 1
     assert L.skc_result_info(None, None, None, None) == 1
+    assert L.skc_autotune(None, None, None, 0, None, None) == 1
+    assert L.skc_dataset_signature(None, None, None, None) == 1
+    assert L.skc_tuning_count(None, None) == 1
+    assert L.skc_tuning_clear(None) == 1
+    assert L.skc_plan_create(None, None, None, None) == 1
+    assert L.skc_plan_execute(None, None) == 1
+    assert L.skc_plan_info(None, None, None, None, None) == 1
+    assert L.skc_dataset_update(None, None) == 1
     assert b"NULL" in L.skc_last_error()
 
 

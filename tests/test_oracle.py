@@ -61,3 +61,24 @@ def test_oracle_matches_reference_live(kind, n, d, max_d, seed):
     for c in a[0]:
         assert np.array_equal(a[0][c], b[0][c])
         assert np.array_equal(a[1][c], b[1][c])
+
+
+@pytest.mark.parametrize("kind,seed,K", [("ties", 41, 4), ("uniform", 42, 16), ("correlated_q", 43, 1),
+                                          ("anticorrelated", 44, 64)])
+def test_prefilter_keeps_full_space_statuses(kind, seed, K):
+    """The exactness argument of the pruner prefilter, on the CPU: dropping
+    every point that one of K pruners strictly dominates leaves the
+    full-space skyline and extended skyline unchanged (the survivors'
+    statuses over the survivors equal their statuses over all points)."""
+    x = datagen.generate(kind, 3000, 6, seed)
+    pruners = x[np.argsort(x.sum(1), kind="stable")[:K]]
+    dropped = np.zeros(len(x), bool)
+    for t in pruners:
+        dropped |= np.all(t < x, axis=1)
+    assert dropped.any()
+    keep = np.nonzero(~dropped)[0].astype(np.uint32)
+    full = (1 << 6) - 1
+    sky, ext = oracle.stsc(x)
+    fsky, fext = oracle.stsc(x[keep])
+    assert np.array_equal(keep[fsky[full]], sky[full])
+    assert np.array_equal(keep[fext[full]], ext[full])
