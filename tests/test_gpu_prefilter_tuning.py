@@ -123,8 +123,10 @@ def test_autotune_stores_and_applies(gpu_ctx):
         assert params["chunk"] in (1, 4, 16)
         assert params["blocks_per_sm"] in (0, 1, 2)
         assert gpu_ctx.tuning_count() == 1
-        # A dataset with the same signature (another seed) picks the tuning up.
-        x2 = datagen.generate("ties", 60000, 8, 6)
+        # Another dataset with the same signature picks the tuning up: the
+        # points scaled by 2 (exact in float32, so every comparison, tie and
+        # the sample signature are unchanged).
+        x2 = x * np.float32(2.0)
         ds2 = sk.Dataset(gpu_ctx, x2)
         assert sk.signature(ds2) == sk.signature(ds)
         sky, ext = oracle.stsc(x2)
