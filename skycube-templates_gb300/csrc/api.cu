@@ -309,8 +309,12 @@ static int run_full_space(Exec& E, skc_dataset* ds, const RunParams& P, Arena& A
   SKC_TRY(A.alloc(&ps.fine, kMaxSortBuckets + 1));
   SKC_TRY(A.alloc(&ps.items, K + 1));
   uint8_t* status;
-  SKC_TRY(A.alloc(&status, n));
+  SKC_TRY(A.alloc(&status, round_up(n, 4)));
   PartitionSkylineArgs pa{list, F.cells, ds->x, ds->n_pad, m_list, n, full, status};
+  // Slices pay on candidate-dense lists (the survivors); on lists full of
+  // dominated points the slices after the strongest partitions would run to
+  // their end for points the first slice already settles.
+  if (list) pa.split_target = (uint32_t)ctx->num_sms * kSplitCtasPerSm;
   SKC_TRY(launch_partition_skyline(s, d, depth, LT, pa, ps));
   T.mark("full: skyline kernel");
 
@@ -528,7 +532,7 @@ static int run_sdsc_plain(Exec& E, skc_dataset* ds, int max_d,
   uint32_t *cand, *d_m, *blk0, *blk1, *cnt;
   uint8_t* status;
   SKC_TRY(A.alloc(&cand, mmax));
-  SKC_TRY(A.alloc(&status, mmax));
+  SKC_TRY(A.alloc(&status, round_up(mmax, 4)));
   SKC_TRY(A.alloc(&d_m, 1));
   const uint64_t nblk = (mmax + 1023) / 1024 + 1;
   SKC_TRY(A.alloc(&blk0, nblk));
@@ -1022,8 +1026,9 @@ static int check_options(skc_dataset* ds, const skc_options* opt, skc_options* o
 // skyline holds every point that can be in S's skyline or extended skyline
 // (a point strictly dominated in the full space is strictly dominated in S),
 // so S is computed over those candidates.
-static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, int depth,
+static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, const RunParams& P,
                              Arena& A, FullSpace& F, skc_result* R, Tracer& T) {
+  const int depth = P.depth;
   cudaStream_t s = E.stream;
   const int d = ds->d;
   const uint32_t nsub = 1u << d, full = nsub - 1;
@@ -1051,17 +1056,42 @@ static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, int depth,
     }
     uint8_t* status;
     uint32_t *blk0, *blk1, *cnt;
-    SKC_TRY(A.alloc(&status, m));
+    SKC_TRY(A.alloc(&status, round_up(m, 4)));
     const uint64_t nblk = (m + 1023) / 1024 + 1;
     SKC_TRY(A.alloc(&blk0, nblk));
     SKC_TRY(A.alloc(&blk1, nblk));
     SKC_TRY(A.alloc(&cnt, 2));
     SKC_TRY(A.alloc(&sky, m));
     SKC_TRY(A.alloc(&ext, m));
-    uint32_t* m_ptr = F.counts + 2;
-    PartitionSkylineArgs pa{F.cand, F.cells, ds->x, ds->n_pad, m_ptr, m, S, status};
+    const uint32_t* list = F.cand;
+    const uint32_t* m_ptr = F.counts + 2;
+    const bool filter = P.pq_size > 0 && m > 2ull * (uint64_t)P.pq_size;
+    if (filter) {
+      // The prefilter on S over the full-space candidates (same argument as
+      // in the full space: every dominator of a survivor on S survives).
+      const uint32_t Kq = (uint32_t)P.pq_size;
+      PrefilterScratch pf;
+      SKC_TRY(A.alloc(&pf.hist, prefilter_sum_bins()));
+      SKC_TRY(A.alloc(&pf.sel, 8));
+      SKC_TRY(A.alloc(&pf.pr_ids, Kq));
+      SKC_TRY(A.alloc(&pf.pr_key, Kq));
+      SKC_TRY(A.alloc(&pf.pr_cells, Kq));
+      SKC_TRY(A.alloc(&pf.pr_x, (uint64_t)d * Kq));
+      SKC_TRY(A.alloc(&pf.st, m));
+      SKC_TRY(A.alloc(&pf.blk0, nblk));
+      SKC_TRY(A.alloc(&pf.blk1, nblk));
+      uint32_t *surv, *d_ns;
+      SKC_TRY(A.alloc(&surv, m));
+      SKC_TRY(A.alloc(&d_ns, 1));
+      PrefilterArgs pfa{F.cells, ds->x, ds->n_pad, F.cand, m_ptr, m, S, Kq, pf};
+      SKC_TRY(launch_prefilter(s, d, E.ctx->num_sms, pfa, surv, d_ns));
+      list = surv;
+      m_ptr = d_ns;
+    }
+    PartitionSkylineArgs pa{list, F.cells, ds->x, ds->n_pad, m_ptr, m, S, status};
+    if (filter) pa.split_target = (uint32_t)E.ctx->num_sms * kSplitCtasPerSm;
     SKC_TRY(launch_partition_skyline(s, d, depth, LT, pa, ps));
-    SKC_TRY(launch_status_compact(s, status, F.cand, m_ptr, m, 0, blk0, blk1, sky, ext, cnt, cnt + 1));
+    SKC_TRY(launch_status_compact(s, status, list, m_ptr, m, 0, blk0, blk1, sky, ext, cnt, cnt + 1));
     uint32_t h[2] = {0, 0};
     SKC_CUDA(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s));
     SKC_CUDA(cudaStreamSynchronize(s));
@@ -1126,7 +1156,7 @@ static int skycube_exec(Exec& E, skc_dataset* ds, const skc_options* opt, skc_re
     if (st == SKC_OK) {
       R->n_cand = F.h_counts[2];
       if (o.subspace) {
-        st = run_single_cuboid(E, ds, o.subspace, depth, A, F, R, T);
+        st = run_single_cuboid(E, ds, o.subspace, P, A, F, R, T);
       } else if (o.algo == SKC_ALGO_SDSC && o.mode == SKC_MODE_PLAIN) {
         st = run_sdsc_plain(E, ds, max_d, depth, A, F, R, T);
       } else {

@@ -115,8 +115,11 @@ struct PartitionSkylineArgs {
   const uint32_t* m_ptr;
   uint64_t m_max;
   uint32_t S;
-  uint8_t* status;      // list position -> status
+  uint8_t* status;      // list position -> status; m_max rounded up to 4 bytes
+  uint32_t split_target = 0;  // CTAs the skyline kernel's work is cut into (0: no slicing)
 };
+// Skyline kernel: CTAs per SM the work is balanced over (split_target).
+constexpr uint32_t kSplitCtasPerSm = 32;
 int launch_mask_keys(cudaStream_t s, const uint4* cells, const uint32_t* ids,
                      const uint32_t* m_ptr, uint64_t m_max, uint32_t S, int d,
                      int B, int depth, int sub_bits, const uint32_t* rank,

@@ -17,6 +17,8 @@
 // tests its point against every staged point with the grid-cell SWAR test
 // and, when cells tie, exact float32 comparisons (see skyline.cu). A
 // strictly dominated point stops; the CTA stops when all its points have.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace skc {
@@ -121,8 +123,78 @@ struct PartKernelArgs {
   const uint32_t* sub_off;  // mask -> range in sub_list
   const uint32_t* sub_list; // ranks of submasks, level order
   uint32_t K;
-  uint8_t* status;          // list position -> status
+  uint8_t* status;          // list position -> status (zeroed, 4-byte padded)
+  const uint32_t* splits;   // slices per work item of partition b [K]
+  const uint32_t* cta_off;  // first CTA of partition b [K + 1]
 };
+
+constexpr uint32_t kMaxSplits = 64;
+constexpr uint64_t kMinSliceWork = 256;  // q's (one tile): below this a slice is not worth a CTA
+
+// Work-proportional slicing of the skyline kernel's items (one CTA of 1024
+// threads, thread b = partition rank b). An item of partition b scans the
+// points of every partition under b's mask, so its cost is work[b] = their
+// count, the same for all of b's items. With W = max(total work / target,
+// kMinSliceWork), each item of b gets ceil(work[b] / W) slices (at most
+// kMaxSplits), so the heavy items of high-mask partitions no longer set the
+// kernel's duration. cta_off is the exclusive prefix of CTAs per partition.
+__global__ void __launch_bounds__(1024) k_split_plan(const uint32_t* __restrict__ boff,
+                                                     const uint32_t* __restrict__ items,
+                                                     const uint32_t* __restrict__ unrank,
+                                                     const uint32_t* __restrict__ sub_off,
+                                                     const uint32_t* __restrict__ sub_list,
+                                                     uint32_t K, uint32_t target,
+                                                     uint32_t* __restrict__ splits,
+                                                     uint32_t* __restrict__ cta_off) {
+  __shared__ unsigned long long s_total;
+  __shared__ uint32_t wsum[32];
+  const uint32_t b = threadIdx.x;
+  const int lane = b & 31, wid = b >> 5;
+  if (b == 0) s_total = 0;
+  __syncthreads();
+  unsigned long long work = 0;
+  uint32_t chunks = 0;
+  if (b < K) {
+    const uint32_t mb = unrank[b];
+    for (uint32_t si = sub_off[mb]; si < sub_off[mb + 1]; ++si) {
+      const uint32_t qb = sub_list[si];
+      work += boff[qb + 1] - boff[qb];
+    }
+    chunks = items[b + 1] - items[b];
+    if (chunks) atomicAdd(&s_total, work * chunks);
+  }
+  __syncthreads();
+  const unsigned long long total = s_total;
+  unsigned long long W = target ? (total + target - 1) / target : ~0ull;
+  if (W < kMinSliceWork) W = kMinSliceWork;
+  uint32_t sb = 1;
+  if (b < K && target) {
+    const unsigned long long q = (work + W - 1) / W;
+    sb = (uint32_t)(q < 1 ? 1 : (q > kMaxSplits ? kMaxSplits : q));
+  }
+  if (b < K) splits[b] = sb;
+  const uint32_t c = b < K ? chunks * sb : 0u;
+  uint32_t inc = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    const uint32_t v = wsum[lane];
+    uint32_t vi = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xffffffffu, vi, o);
+      if (lane >= o) vi += u;
+    }
+    wsum[lane] = vi - v;
+  }
+  __syncthreads();
+  const uint32_t excl = wsum[wid] + inc - c;
+  if (b < K) cta_off[b] = excl;
+  if (b == K - 1) cta_off[K] = excl + c;
+}
 
 // NA = number of attributes of the subspace (all of them are compared).
 //
@@ -134,6 +206,13 @@ struct PartKernelArgs {
 // dominates q lies in a partition under p's mask as well and strictly
 // dominates p. Nothing waits: an unfinished partition is read in full. A CTA
 // publishes its confirmed points, fences, then counts itself in pdone.
+//
+// Slices (k_split_plan). An item of partition b is cut into splits[b] CTAs,
+// each taking an equal slice of the concatenated submask partitions; the
+// slices' statuses combine by a byte-wise atomic OR of bit flags (1
+// dominated, 2 strictly dominated; 3 reads as strictly dominated). A sliced
+// partition neither publishes nor uses confirmed lists (no CTA knows its
+// points' final status); the others still do.
 template <int NA>
 __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
   constexpr int NW = (NA + 3) / 4;
@@ -142,16 +221,21 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
   __shared__ float q_x[NA][TQ];
   __shared__ uint32_t s_conf_end;
 
-  const uint32_t nitems = a.items[a.K];
-  if (blockIdx.x >= nitems) return;
-  const uint32_t it = blockIdx.x;  // lattice-level order: lower partitions first
+  __shared__ unsigned long long s_total;
+  // CTAs go in partition rank order (lattice level: lower partitions first).
+  if (blockIdx.x >= a.cta_off[a.K]) return;
   uint32_t lo = 0, hi = a.K;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
-    if (a.items[mid] <= it) lo = mid; else hi = mid;
+    if (a.cta_off[mid] <= blockIdx.x) lo = mid; else hi = mid;
   }
   const uint32_t b = lo;
-  const uint32_t pbeg = a.boff[b] + (it - a.items[b]) * TQ;
+  const uint32_t splits = a.splits[b];
+  const uint32_t local = blockIdx.x - a.cta_off[b];
+  const uint32_t chunk = local / splits;
+  const uint32_t sp = local - chunk * splits;
+  const bool use_conf = a.conf_cells != nullptr && splits == 1;
+  const uint32_t pbeg = a.boff[b] + chunk * TQ;
   const uint32_t pend = min(a.boff[b + 1], pbeg + TQ);
   const uint32_t i = pbeg + threadIdx.x;
   const bool valid = i < pend;
@@ -181,13 +265,38 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
   bool done = !valid;
   bool all_done = false;
   const uint32_t mb = a.unrank[b];
-  const uint32_t s1 = a.sub_off[mb + 1];
-  for (uint32_t si = a.sub_off[mb]; si < s1 && !all_done; ++si) {
+  const uint32_t s0 = a.sub_off[mb], s1 = a.sub_off[mb + 1];
+  // This CTA's slice [s_lo, s_hi) of the concatenated submask partitions.
+  uint64_t s_lo = 0, s_hi = ~0ull;
+  if (splits > 1) {
+    if (threadIdx.x == 0) s_total = 0;
+    __syncthreads();
+    unsigned long long part = 0;
+    for (uint32_t si = s0 + threadIdx.x; si < s1; si += blockDim.x) {
+      const uint32_t qb = a.sub_list[si];
+      part += a.boff[qb + 1] - a.boff[qb];
+    }
+    if (part) atomicAdd(&s_total, part);
+    __syncthreads();
+    const uint64_t total = s_total;
+    s_lo = total * sp / splits;
+    s_hi = total * (sp + 1) / splits;
+  }
+  uint64_t acc = 0;  // q's of the partitions before si (uniform over the CTA)
+  for (uint32_t si = s0; si < s1 && !all_done && acc < s_hi; ++si) {
     const uint32_t qb = a.sub_list[si];
-    const uint32_t qbeg = a.boff[qb];
+    uint32_t qbeg = a.boff[qb];
     uint32_t qend = a.boff[qb + 1];
+    if (splits > 1) {
+      const uint64_t start = acc, sz = qend - qbeg;
+      acc += sz;
+      const uint64_t c0 = max(s_lo, start), c1 = min(s_hi, start + sz);
+      if (c0 >= c1) continue;
+      qend = qbeg + (uint32_t)(c1 - start);
+      qbeg = qbeg + (uint32_t)(c0 - start);
+    }
     bool conf = false;
-    if (a.conf_cells && qb != b) {
+    if (use_conf && qb != b) {
       if (threadIdx.x == 0) {
         uint32_t e = 0xffffffffu;
         const uint32_t need = a.items[qb + 1] - a.items[qb];
@@ -263,8 +372,15 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
       __syncthreads();
     }
   }
-  if (valid) a.status[a.sorted[i]] = st;
-  if (a.conf_cells) {
+  if (valid) {
+    const uint32_t pos = a.sorted[i];
+    if (splits == 1)
+      a.status[pos] = st;
+    else if (st)
+      atomicOr(reinterpret_cast<unsigned int*>(a.status + (pos & ~3u)),
+               (unsigned int)st << (8 * (pos & 3u)));
+  }
+  if (use_conf) {
     if (valid && st != 2) {
       const uint32_t slot = a.boff[b] + atomicAdd(&a.ccount[b], 1u);
       a.conf_cells[slot] = my_cells;
@@ -330,13 +446,26 @@ int launch_partition_skyline(cudaStream_t s, int d, int depth,
   k_chunk_counts<<<blocks_for(K, 256, 64), 256, 0, s>>>(ps.counts, K, ps.items);
   SKC_LAUNCH_CHECK();
   SKC_TRY(launch_scan_single_u32(s, ps.items, K));
+  // Slices per item and CTA offsets, in the counting sort's cursor scratch
+  // (free once the partition offsets are extracted): [0, K) and [K, 2K + 1).
+  uint32_t* splits = ps.cursor;
+  uint32_t* cta_off = ps.cursor + K;
+  k_split_plan<<<1, 1024, 0, s>>>(ps.counts, ps.items, T.unrank, T.sub_off, T.sub_list, K,
+                                  a.split_target, splits, cta_off);
+  SKC_LAUNCH_CHECK();
   PartKernelArgs k{ps.conf_cells, ps.conf_x, ps.ccount, ps.pdone, ps.sorted, ps.ccells, ps.cx,
-                   pitch, ps.counts, ps.items, T.unrank, T.sub_off, T.sub_list, K, a.status};
+                   pitch, ps.counts, ps.items, T.unrank, T.sub_off, T.sub_list, K, a.status,
+                   splits, cta_off};
+  // Split CTAs OR their statuses in: start from zero (the buffer is padded
+  // to a multiple of 4 bytes).
+  SKC_CUDA(cudaMemsetAsync(a.status, 0, (a.m_max + 3) & ~3ull, s));
   if (ps.conf_cells) {
     SKC_CUDA(cudaMemsetAsync(ps.ccount, 0, K * sizeof(uint32_t), s));
     SKC_CUDA(cudaMemsetAsync(ps.pdone, 0, K * sizeof(uint32_t), s));
   }
-  const unsigned grid = (unsigned)((a.m_max + 255) / 256 + K);
+  // Upper bound of the CTAs k_split_plan hands out: sum over items of
+  // ceil(work / W) <= target + items.
+  const unsigned grid = (unsigned)((a.m_max + 255) / 256 + K + a.split_target);
 #define SKC_PART_CASE(N)                                  \
   case N:                                                 \
     k_skyline_part<N><<<grid, 256, 0, s>>>(k);            \
