@@ -56,8 +56,11 @@ struct BitState {
   static constexpr bool REG = (W <= 32);   // STRICT in registers
   static constexpr uint32_t AW = NSUB / 2;  // tie-map words (2 entries each)
   static constexpr bool A_SMEM = (D <= 12);  // tie map in shared memory
+  // Above, the map lives in a global slab and is closed chunk by chunk
+  // through a 512-word shared scratch (tie_global_output).
+  static constexpr uint32_t CHUNK_WORDS = A_SMEM ? 0 : 512;
   // shared memory per warp, in words
-  static constexpr uint32_t SMEM_WORDS = (REG ? 0 : W) + (A_SMEM ? AW : 0);
+  static constexpr uint32_t SMEM_WORDS = (REG ? 0 : W) + (A_SMEM ? AW : 0) + CHUNK_WORDS;
 };
 
 // Splits the subsets of h over 32 lanes: `low` = the lowest five set bits of
@@ -109,6 +112,103 @@ __device__ void tie_closure(uint32_t* A, int lane) {
       A[w] |= A[w + st];
     }
     __syncwarp();
+  }
+}
+
+// The same closure for a map in the global slab (d >= 13), blocked so that
+// a warp makes tens of memory round trips per candidate instead of one per
+// pass and word. Entries are grouped in chunks of 1024 (512 words): entry
+// bits 0..9 lie inside a chunk, bits 10..d-1 index the chunk.
+//
+// Phase 1: the chunk-index bits, in groups of up to four. For one group a
+// lane holds, in registers, the same word of the 2^GB chunks that differ
+// only in the group's bits (coalesced over the warp: word 32i + lane), ORs
+// each into its subsets (a butterfly), and stores them back.
+template <int GB>
+__device__ __forceinline__ void closure_chunk_bits(uint32_t* A, int lane, int g0, uint32_t nc) {
+  constexpr uint32_t NX = 1u << GB;
+  const uint32_t gmask = (NX - 1) << g0;
+  for (uint32_t base = 0; base < nc; ++base) {
+    if (base & gmask) continue;
+    for (uint32_t i = 0; i < 16; ++i) {
+      uint32_t v[NX];
+#pragma unroll
+      for (uint32_t x = 0; x < NX; ++x) v[x] = A[((base | (x << g0)) << 9) + 32 * i + lane];
+#pragma unroll
+      for (int bit = 0; bit < GB; ++bit)
+#pragma unroll
+        for (uint32_t x = 0; x < NX; ++x)
+          if (!(x & (1u << bit))) v[x] |= v[x | (1u << bit)];
+#pragma unroll
+      for (uint32_t x = 0; x < NX; ++x) A[((base | (x << g0)) << 9) + 32 * i + lane] = v[x];
+    }
+  }
+}
+
+// Spreads the 16 bits of x to the even bit positions.
+__device__ __forceinline__ uint32_t spread_even(uint32_t x) {
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+// Phase 2, per chunk: load it into the scratch Cs, close its ten low entry
+// bits there, and turn it straight into the chunk's 32 output words (entry
+// S is tie-dominated iff S meets T[S]): word j of the chunk gives the bits
+// of entries 2j and 2j+1, two ballots over j = 32i + lane give output words
+// 2i (lanes 0..15) and 2i+1 (lanes 16..31) after an even/odd interleave.
+// Lane l ends with output word 32c + l and writes dom and ext for it.
+template <int D>
+__device__ void tie_global_output(uint32_t* A, uint32_t* Cs, const uint32_t* sat_s, int lane,
+                                  uint32_t p, uint32_t* __restrict__ out_dom,
+                                  uint32_t* __restrict__ out_ext) {
+  constexpr int HB = D - 10;
+  constexpr uint32_t NC = 1u << HB;
+  constexpr uint32_t W = (1u << D) / 32;
+  closure_chunk_bits<(HB < 4 ? HB : 4)>(A, lane, 0, NC);
+  if constexpr (HB > 4) closure_chunk_bits<HB - 4>(A, lane, 4, NC);
+  __syncwarp();
+  for (uint32_t c = 0; c < NC; ++c) {
+#pragma unroll
+    for (uint32_t k = 0; k < 16; ++k) {
+      const uint32_t x = A[(c << 9) + 32 * k + lane];
+      Cs[32 * k + lane] = x | (x >> 16);  // entry bit 0 (inside the word)
+    }
+    __syncwarp();
+    for (int j = 1; j <= 9; ++j) {  // entry bit j: words w and w + 2^(j-1)
+      const uint32_t st = 1u << (j - 1);
+#pragma unroll
+      for (uint32_t t = lane; t < 256; t += 32) {
+        const uint32_t w = ((t >> (j - 1)) << j) | (t & (st - 1));
+        Cs[w] |= Cs[w + st];
+      }
+      __syncwarp();
+    }
+    uint32_t mine = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < 16; ++i) {
+      const uint32_t j = 32 * i + lane;
+      const uint32_t x = Cs[j];
+      const uint32_t e0 = (c << 10) + 2 * j;
+      const uint32_t ev = __ballot_sync(kFull, (e0 & x & 0xffffu) != 0u);
+      const uint32_t od = __ballot_sync(kFull, ((e0 + 1) & (x >> 16)) != 0u);
+      const uint32_t lo = spread_even(ev & 0xffffu) | (spread_even(od & 0xffffu) << 1);
+      const uint32_t hi = spread_even(ev >> 16) | (spread_even(od >> 16) << 1);
+      if ((uint32_t)lane == 2 * i) mine = lo;
+      if ((uint32_t)lane == 2 * i + 1) mine = hi;
+    }
+    const uint32_t t = 32 * c + lane;
+    const uint32_t s_ = sat_s[t];
+    uint32_t dom = s_ | mine, ext = mine & ~s_;
+    if (t == 0) {
+      dom &= ~1u;
+      ext &= ~1u;
+    }
+    out_dom[(uint64_t)p * W + t] = dom;
+    if (out_ext) out_ext[(uint64_t)p * W + t] = ext;
+    __syncwarp();  // Cs is reused by the next chunk
   }
 }
 
@@ -323,6 +423,14 @@ __global__ void __launch_bounds__(256) k_bitmaps(
 
     // Output: dominated = STRICT | TIE, extended = TIE \ STRICT, with TIE
     // from the closed tie map. Bit 0 (the empty subspace) is cleared.
+    if constexpr (!BS::A_SMEM) {
+      if (touched) {
+        __syncwarp();
+        tie_global_output<D>(A, wsm + W, sat_s, lane, p, out_dom, out_ext);
+        __syncwarp();
+        continue;
+      }
+    }
     if (touched) {
       __syncwarp();
       tie_closure<D>(A, lane);
