@@ -122,7 +122,7 @@ struct PartitionSkylineArgs {
 constexpr uint32_t kSplitCtasPerSm = 32;
 int launch_mask_keys(cudaStream_t s, const uint4* cells, const uint32_t* ids,
                      const uint32_t* m_ptr, uint64_t m_max, uint32_t S, int d,
-                     int B, int depth, int sub_bits, const uint32_t* rank,
+                     int B, int depth, int sub_bits, int sub_mode, const uint32_t* rank,
                      uint32_t* keys);
 int launch_partition_offsets(cudaStream_t s, const uint32_t* fine, uint32_t K, int sub_bits,
                              uint32_t* boff);

@@ -27,12 +27,16 @@ namespace skc {
 // attributes of S, times 2^sub_bits, plus (when sub_bits > 0) the sum of its
 // grid cells over S scaled to sub_bits bits. Sorting by the key groups
 // points by partition and, inside a partition, from strong to weak, so
-// points that survive long share warps. Only the partition part matters for
-// correctness.
+// points that survive long share warps. With sub_mode 1 the sub-key is
+// instead the quartile-cell bit (the cell bit below the median bit) of the
+// first sub_bits attributes of S, attribute 0 most significant: consecutive
+// points then share their quartile on most attributes, which keeps the
+// minimum-cell boxes of 32-point blocks tight. Only the partition part
+// matters for correctness.
 __global__ void k_mask_keys(const uint4* __restrict__ cells,
                             const uint32_t* __restrict__ ids,
                             const uint32_t* __restrict__ m_ptr, uint32_t S,
-                            int d, int B, int depth, int sub_bits,
+                            int d, int B, int depth, int sub_bits, int sub_mode,
                             const uint32_t* __restrict__ rank,
                             uint32_t* __restrict__ keys) {
   const uint32_t m = *m_ptr;
@@ -43,17 +47,19 @@ __global__ void k_mask_keys(const uint4* __restrict__ cells,
        i += gridDim.x * blockDim.x) {
     const uint32_t id = ids ? ids[i] : i;
     const uint4 c = cells[id];
-    uint32_t cm = 0, csum = 0;
+    uint32_t cm = 0, csum = 0, qpat = 0;
     int j = 0;
     for (int k = 0; k < d; ++k) {
       if (!(S & (1u << k))) continue;
       const uint32_t cell = (word_of(c, k >> 2) >> (8 * (k & 3))) & 0x7fu;
       if (j < B) cm |= ((cell >> sh) & 1u) << j;
+      if (j < sub_bits && sh >= 1) qpat |= ((cell >> (sh - 1)) & 1u) << (sub_bits - 1 - j);
       csum += cell;
       ++j;
     }
     uint32_t key = rank[cm] << sub_bits;
-    if (sub_bits && span) key |= (csum * ((1u << sub_bits) - 1)) / span;
+    if (sub_mode == 1) key |= qpat;
+    else if (sub_bits && span) key |= (csum * ((1u << sub_bits) - 1)) / span;
     keys[i] = key;
   }
 }
@@ -397,10 +403,10 @@ static inline unsigned blocks_for(uint64_t items, int threads, int cap);
 
 int launch_mask_keys(cudaStream_t s, const uint4* cells, const uint32_t* ids,
                      const uint32_t* m_ptr, uint64_t m_max, uint32_t S, int d,
-                     int B, int depth, int sub_bits, const uint32_t* rank,
+                     int B, int depth, int sub_bits, int sub_mode, const uint32_t* rank,
                      uint32_t* keys) {
   k_mask_keys<<<blocks_for(m_max, 256, 152 * 8), 256, 0, s>>>(cells, ids, m_ptr, S, d, B, depth,
-                                                               sub_bits, rank, keys);
+                                                               sub_bits, sub_mode, rank, keys);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }
@@ -434,7 +440,7 @@ int launch_partition_skyline(cudaStream_t s, int d, int depth,
   bs.counts = ps.fine;
   bs.cursor = ps.cursor;
   k_mask_keys<<<blocks_for(a.m_max, 256, 152 * 8), 256, 0, s>>>(
-      a.cells, a.ids, a.m_ptr, a.S, d, T.B, depth, sub_bits, T.rank, ps.keys);
+      a.cells, a.ids, a.m_ptr, a.S, d, T.B, depth, sub_bits, 0, T.rank, ps.keys);
   SKC_LAUNCH_CHECK();
   SKC_TRY(launch_counting_sort(s, ps.keys, a.m_ptr, a.m_max, KB, bs, ps.sorted, nullptr));
   k_partition_offsets<<<blocks_for(K + 1, 256, 64), 256, 0, s>>>(ps.fine, K, sub_bits, ps.counts);
