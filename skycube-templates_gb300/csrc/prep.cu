@@ -105,42 +105,55 @@ __global__ void k_hist(const uint32_t* __restrict__ keys,
 }
 
 // In-place exclusive scan of a[0 .. len) with one CTA of 1024 threads;
-// a[len] receives the total. len + 1 entries must be allocated.
+// a[len] receives the total. len + 1 entries must be allocated. The array is
+// walked in tiles of 4096 (4 consecutive entries per thread, so each warp
+// reads and writes 512 contiguous bytes), each tile scanned in the block and
+// offset by the running total of the tiles before it.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_scan_single(T* __restrict__ a,
                                                       uint32_t len) {
-  __shared__ T warp_tot[32];
-  const uint32_t per = (len + 1023) / 1024;
-  const uint32_t beg = threadIdx.x * per;
-  const uint32_t end = min(len, beg + per);
-  T local = 0;
-  for (uint32_t i = beg; i < end; ++i) local += a[i];
-  // block exclusive scan of `local`
+  __shared__ T warp_excl[32];
+  __shared__ T tile_tot;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  T incl = local;
-  for (int o = 1; o < 32; o <<= 1) {
-    T v = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += v;
-  }
-  if (lane == 31) warp_tot[wid] = incl;
-  __syncthreads();
-  if (wid == 0) {
-    T v = warp_tot[lane];
-    T s = v;
-    for (int o = 1; o < 32; o <<= 1) {
-      T u = __shfl_up_sync(0xffffffffu, s, o);
-      if (lane >= o) s += u;
+  T carry = 0;  // total of the tiles before this one (same in every thread)
+  for (uint32_t base = 0; base < len; base += 4096) {
+    T v[4];
+    T local = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t i = base + 4 * threadIdx.x + j;
+      v[j] = i < len ? a[i] : T(0);
+      local += v[j];
     }
-    warp_tot[lane] = s - v;  // exclusive
+    T incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+      const T u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane == 31) warp_excl[wid] = incl;  // warp totals for now
+    __syncthreads();
+    if (wid == 0) {
+      const T w = warp_excl[lane];
+      T sw = w;
+      for (int o = 1; o < 32; o <<= 1) {
+        const T u = __shfl_up_sync(0xffffffffu, sw, o);
+        if (lane >= o) sw += u;
+      }
+      warp_excl[lane] = sw - w;
+      if (lane == 31) tile_tot = sw;
+    }
+    __syncthreads();
+    T run = carry + warp_excl[wid] + incl - local;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t i = base + 4 * threadIdx.x + j;
+      if (i < len) a[i] = run;
+      run += v[j];
+    }
+    carry += tile_tot;
+    __syncthreads();  // warp_excl and tile_tot are reused by the next tile
   }
-  __syncthreads();
-  T run = warp_tot[wid] + incl - local;
-  for (uint32_t i = beg; i < end; ++i) {
-    T v = a[i];
-    a[i] = run;
-    run += v;
-  }
-  if (threadIdx.x == 1023) a[len] = warp_tot[31] + incl;
+  if (threadIdx.x == 0) a[len] = carry;
 }
 
 // Scatters item i to its bucket. sorted[pos] = i; hi[pos] = end of i's
