@@ -27,12 +27,15 @@ namespace skc {
 // attributes of S, times 2^sub_bits, plus (when sub_bits > 0) the sum of its
 // grid cells over S scaled to sub_bits bits. Sorting by the key groups
 // points by partition and, inside a partition, from strong to weak, so
-// points that survive long share warps. With sub_mode 1 the sub-key is
-// instead the quartile-cell bit (the cell bit below the median bit) of the
-// first sub_bits attributes of S, attribute 0 most significant: consecutive
-// points then share their quartile on most attributes, which keeps the
-// minimum-cell boxes of 32-point blocks tight. Only the partition part
-// matters for correctness.
+// points that survive long share warps. With sub_mode 1 the sub-key orders
+// points by the quartile-cell bits (the cell bit below the median bit) of
+// the first sub_bits attributes of S, as a Gray code: a point's pattern is
+// ranked by its position in the reflected binary sequence (the prefix XOR of
+// its bits, attribute 0 most significant), so consecutive patterns differ in
+// one attribute and any run of them varies in few. Consecutive points then
+// share their quartile on most attributes, which keeps the minimum-cell
+// boxes of 32-point blocks tight. Only the partition part matters for
+// correctness.
 __global__ void k_mask_keys(const uint4* __restrict__ cells,
                             const uint32_t* __restrict__ ids,
                             const uint32_t* __restrict__ m_ptr, uint32_t S,
@@ -58,7 +61,11 @@ __global__ void k_mask_keys(const uint4* __restrict__ cells,
       ++j;
     }
     uint32_t key = rank[cm] << sub_bits;
-    if (sub_mode == 1) key |= qpat;
+    if (sub_mode == 1) {
+      uint32_t g = qpat;  // rank of qpat in the Gray sequence
+      for (int s2 = 1; s2 < 32; s2 <<= 1) g ^= g >> s2;
+      key |= g;
+    }
     else if (sub_bits && span) key |= (csum * ((1u << sub_bits) - 1)) / span;
     keys[i] = key;
   }
