@@ -371,10 +371,35 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   SKC_TRY(A.alloc(&bmin, (m + 31) / 32));
   SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, F.cand, m_ptr, m, depth, pivots, cc));
 
+  // q list: the full-space skyline only. If a point q' weakly dominates q
+  // (q' <= q on every attribute), then for every p, LT(q, p) and LE(q, p)
+  // are subsets of LT(q', p) and LE(q', p), so q's strict and tie sets are
+  // inside q''s; following such q' ends at a skyline point. The
+  // extended-skyline candidates are therefore p's only (on tie-heavy data
+  // they are nearly all candidates: 581k x 10 ties has 9 skyline points
+  // among 24,446 candidates). q's are kept as positions in candidate order;
+  // their count stays on the device.
+  uint32_t *qpos, *mq_ptr;
+  SKC_TRY(A.alloc(&qpos, m));
+  SKC_TRY(A.alloc(&mq_ptr, 1));
+  {
+    const uint64_t nb = (m + 1023) / 1024 + 1;
+    uint8_t* qst;
+    uint32_t *b0, *b1;
+    SKC_TRY(A.alloc(&qst, m));
+    SKC_TRY(A.alloc(&b0, nb));
+    SKC_TRY(A.alloc(&b1, nb));
+    SKC_TRY(launch_member_flags(s, F.cand, m_ptr, m, F.sky, F.counts + 0, qst));
+    SKC_TRY(launch_status_compact(s, qst, nullptr, m_ptr, m, 1, b0, b1, qpos, nullptr, mq_ptr,
+                                  nullptr));
+  }
+  // Host-side size of the q list (plans know only the candidate capacity).
+  const uint64_t mq_host = E.plan ? m : F.h_counts[0];
+
   // q order: partitions by median mask over the first B attributes, in
   // lattice-level order (strongest partitions first).
   LevelTables LT;
-  SKC_TRY(level_tables(ctx, bitmap_partition_dims(d, m, P.tile_points), &LT));
+  SKC_TRY(level_tables(ctx, bitmap_partition_dims(d, mq_host, P.tile_points), &LT));
   // Inside a partition, q's are ordered by the quartile-cell bits of the
   // first 8 attributes in Gray-code order, so consecutive q's share their
   // quartile on most attributes and the 32-q blocks' minimum-cell boxes stay
@@ -392,18 +417,20 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   SKC_TRY(A.alloc(&b.counts, KB + 1));
   SKC_TRY(A.alloc(&b.cursor, KB + 1));
   SKC_TRY(A.alloc(&boff, K + 1));
-  uint32_t *qperm, *qids;
+  uint32_t *qperm, *qidx, *qids;
   SKC_TRY(A.alloc(&qperm, m));
+  SKC_TRY(A.alloc(&qidx, m));
   SKC_TRY(A.alloc(&qids, m));
-  SKC_TRY(launch_mask_keys(s, cc, nullptr, m_ptr, m, nsub - 1, d, LT.B, depth, sub_bits,
+  SKC_TRY(launch_mask_keys(s, cc, qpos, mq_ptr, m, nsub - 1, d, LT.B, depth, sub_bits,
                            depth >= 2 ? 1 : 0,
                            LT.rank, b.keys));
-  SKC_TRY(launch_counting_sort(s, b.keys, m_ptr, m, KB, b, qperm, nullptr));
+  SKC_TRY(launch_counting_sort(s, b.keys, mq_ptr, m, KB, b, qperm, nullptr));
   SKC_TRY(launch_partition_offsets(s, b.counts, K, sub_bits, boff));
-  SKC_TRY(launch_gather_u32(s, F.cand, qperm, m_ptr, m, qids));
-  SKC_TRY(launch_gather_soa(s, ds->x, ds->n_pad, d, qids, m_ptr, m, m_pad, xq));
-  SKC_TRY(launch_gather_u4(s, cc, qperm, m_ptr, m, qc));
-  SKC_TRY(launch_block_min(s, qc, m_ptr, m, bmin));
+  SKC_TRY(launch_gather_u32(s, qpos, qperm, mq_ptr, m, qidx));  // q order -> candidate position
+  SKC_TRY(launch_gather_u32(s, F.cand, qidx, mq_ptr, m, qids));
+  SKC_TRY(launch_gather_soa(s, ds->x, ds->n_pad, d, qids, mq_ptr, m, m_pad, xq));
+  SKC_TRY(launch_gather_u4(s, cc, qidx, mq_ptr, m, qc));
+  SKC_TRY(launch_block_min(s, qc, mq_ptr, m, bmin));
 
   T.mark("cand: cells+q order");
   uint32_t *dom, *ext = nullptr, *work;
@@ -416,7 +443,7 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   SKC_TRY(bitmap_tie_slab_words(d, ctx->num_sms, &slab_words));
   if (slab_words) SKC_TRY(A.alloc(&slab, slab_words));
   BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, boff, LT.unrank, K, LT.B, depth,
-                m_ptr, work, (uint32_t)P.chunk, 0xffffffffu, dom, ext,
+                m_ptr, mq_ptr, work, (uint32_t)P.chunk, 0xffffffffu, dom, ext,
                 P.blocks_per_sm * ctx->num_sms, slab};
   if (o.mode == SKC_MODE_BATCHED) {
     SKC_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), s));

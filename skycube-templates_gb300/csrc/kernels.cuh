@@ -53,6 +53,9 @@ int launch_merge_disjoint(cudaStream_t s, const uint32_t* a, uint32_t na,
                           const uint32_t* b, uint32_t nb, uint32_t* out);
 int launch_gather_u32(cudaStream_t s, const uint32_t* in, const uint32_t* perm,
                       const uint32_t* m_ptr, uint64_t m_max, uint32_t* out);
+int launch_member_flags(cudaStream_t s, const uint32_t* list, const uint32_t* m_ptr,
+                        uint64_t m_max, const uint32_t* sorted_set, const uint32_t* nset_ptr,
+                        uint8_t* st);
 int launch_sample_signature(cudaStream_t s, const float* x, uint64_t n_pad, uint64_t n, int d,
                             uint32_t* out);
 int launch_cap_count(cudaStream_t s, uint32_t* m_ptr, uint32_t cap, uint64_t* stats, int slot);
@@ -173,7 +176,8 @@ struct BitmapArgs {
   uint32_t K;
   int B;
   int depth;
-  const uint32_t* m_ptr;
+  const uint32_t* m_ptr;   // candidates (p's)
+  const uint32_t* mq_ptr;  // q's (full-space skyline members, q order)
   uint32_t* work;        // work counter, must hold p_begin
   uint32_t chunk;        // candidates per work-counter grab (0: 1)
   uint32_t p_end;        // stop at min(m, p_end)

@@ -732,4 +732,31 @@ int launch_stat_u64(cudaStream_t s, const uint64_t* src, uint64_t* stats, int sl
   return SKC_OK;
 }
 
+// st[i] = 0 when list[i] occurs in sorted_set[0 .. *nset_ptr) (ascending),
+// else 2: status-compaction input that keeps the members.
+__global__ void k_member_flags(const uint32_t* __restrict__ list,
+                               const uint32_t* __restrict__ m_ptr,
+                               const uint32_t* __restrict__ sorted_set,
+                               const uint32_t* __restrict__ nset_ptr,
+                               uint8_t* __restrict__ st) {
+  const uint32_t m = *m_ptr, ns = *nset_ptr;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const uint32_t v = list[i];
+    uint32_t lo = 0, hi = ns;  // first position with sorted_set[pos] >= v
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (sorted_set[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    st[i] = (lo < ns && sorted_set[lo] == v) ? 0 : 2;
+  }
+}
+
+int launch_member_flags(cudaStream_t s, const uint32_t* list, const uint32_t* m_ptr,
+                        uint64_t m_max, const uint32_t* sorted_set, const uint32_t* nset_ptr,
+                        uint8_t* st) {
+  k_member_flags<<<grid_for(m_max, 256, 152 * 8), 256, 0, s>>>(list, m_ptr, sorted_set, nset_ptr, st);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
 }  // namespace skc
