@@ -59,8 +59,13 @@ struct BitState {
   // Above, the map lives in a global slab and is closed chunk by chunk
   // through a 512-word shared scratch (tie_global_output).
   static constexpr uint32_t CHUNK_WORDS = A_SMEM ? 0 : 512;
+  // Also above: the first LIST_WORDS tie pairs of a candidate are kept as a
+  // list (E | L << 16) and applied directly when no more come; the global
+  // map is used only when a candidate has more.
+  static constexpr uint32_t LIST_WORDS = A_SMEM ? 0 : 32;
   // shared memory per warp, in words
-  static constexpr uint32_t SMEM_WORDS = (REG ? 0 : W) + (A_SMEM ? AW : 0) + CHUNK_WORDS;
+  static constexpr uint32_t SMEM_WORDS =
+      (REG ? 0 : W) + (A_SMEM ? AW : 0) + CHUNK_WORDS + LIST_WORDS;
 };
 
 // Splits the subsets of h over 32 lanes: `low` = the lowest five set bits of
@@ -293,6 +298,9 @@ __global__ void __launch_bounds__(256) k_bitmaps(
       __syncwarp();
     }
     bool touched = false;  // tie map in use for this p
+    // d >= 13: 0 no tie pair, 1 pairs in the list, 2 pairs in the global map
+    int tmode = 0;
+    uint32_t tcount = 0;  // pairs in the list (same in every lane)
     auto in_strict = [&](uint32_t S) -> bool {
       uint32_t word;
       if (REG) word = __shfl_sync(kFull, sat, S >> 5);
@@ -385,13 +393,38 @@ __global__ void __launch_bounds__(256) k_bitmaps(
             // Tie pairs go to the tie map (one atomic per lane); a tie set
             // inside STRICT changes nothing.
             const bool tie_lane = !hit && le != lt && !t_le;
-            if (__any_sync(kFull, tie_lane)) {
-              if (!touched) {
-                for (uint32_t w = lane; w < AW; w += 32) A[w] = 0;
-                __syncwarp();
-                touched = true;
+            const uint32_t tb = __ballot_sync(kFull, tie_lane);
+            if (tb) {
+              if constexpr (BS::A_SMEM) {
+                if (!touched) {
+                  for (uint32_t w = lane; w < AW; w += 32) A[w] = 0;
+                  __syncwarp();
+                  touched = true;
+                }
+                if (tie_lane) atomicOr(&A[le >> 1], lt << (16 * (le & 1)));
+              } else {
+                uint32_t* tlist = wsm + W + BS::CHUNK_WORDS;
+                const uint32_t nt = __popc(tb);
+                if (tmode != 2 && tcount + nt <= BS::LIST_WORDS) {
+                  if (tie_lane) tlist[tcount + __popc(tb & ((1u << lane) - 1u))] = le | (lt << 16);
+                  tcount += nt;
+                  tmode = 1;
+                  __syncwarp();
+                } else {
+                  if (tmode != 2) {
+                    // Too many pairs: move to the global map (zeroed, then
+                    // the listed pairs OR-ed in).
+                    for (uint32_t w = lane; w < AW; w += 32) A[w] = 0;
+                    __syncwarp();
+                    if ((uint32_t)lane < tcount) {
+                      const uint32_t e = tlist[lane];
+                      atomicOr(&A[(e & 0xffffu) >> 1], (e >> 16) << (16 * (e & 1u)));
+                    }
+                    tmode = 2;
+                  }
+                  if (tie_lane) atomicOr(&A[le >> 1], lt << (16 * (le & 1)));
+                }
               }
-              if (tie_lane) atomicOr(&A[le >> 1], lt << (16 * (le & 1)));
             }
             // Strict updates: down(LT) into STRICT, one pair at a time.
             uint32_t todo = __ballot_sync(kFull, !hit && !t_lt);
@@ -426,9 +459,34 @@ __global__ void __launch_bounds__(256) k_bitmaps(
     // Output: dominated = STRICT | TIE, extended = TIE \ STRICT, with TIE
     // from the closed tie map. Bit 0 (the empty subspace) is cleared.
     if constexpr (!BS::A_SMEM) {
-      if (touched) {
+      if (tmode == 2) {
         __syncwarp();
         tie_global_output<D>(A, wsm + W, sat_s, lane, p, out_dom, out_ext);
+        __syncwarp();
+        continue;
+      }
+      if (tmode == 1) {
+        // Few pairs: word w of each pair's tie set down(E) \ down(E \ L)
+        // is submask(E & 31) when w is a subset of E >> 5, minus
+        // submask(F & 31) when w is also a subset of F >> 5, F = E \ L.
+        const uint32_t* tlist = wsm + W + BS::CHUNK_WORDS;
+        for (uint32_t w = lane; w < W; w += 32) {
+          uint32_t t_ = 0;
+          for (uint32_t j = 0; j < tcount; ++j) {
+            const uint32_t e = tlist[j];
+            const uint32_t E = e & 0xffffu, F = E & ~(e >> 16);
+            if ((w & ~(E >> 5)) == 0u)
+              t_ |= c_submask[E & 31] & (((w & ~(F >> 5)) == 0u) ? ~c_submask[F & 31] : ~0u);
+          }
+          const uint32_t s_ = sat_s[w];
+          uint32_t dom = s_ | t_, ext = t_ & ~s_;
+          if (w == 0) {
+            dom &= ~1u;
+            ext &= ~1u;
+          }
+          out_dom[(uint64_t)p * W + w] = dom;
+          if (out_ext) out_ext[(uint64_t)p * W + w] = ext;
+        }
         __syncwarp();
         continue;
       }
