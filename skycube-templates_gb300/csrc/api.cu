@@ -367,7 +367,7 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   uint4 *cc, *qc, *bmin;
   SKC_TRY(A.alloc(&pivots, (uint64_t)kMaxDims * kMaxPivots));
   SKC_TRY(A.alloc(&cc, m));
-  SKC_TRY(A.alloc(&qc, m));
+  SKC_TRY(A.alloc(&qc, round_up(m, 32)));  // padded to whole blocks (k_pad_q)
   SKC_TRY(A.alloc(&bmin, (m + 31) / 32));
   SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, F.cand, m_ptr, m, depth, pivots, cc));
 
@@ -430,6 +430,7 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   SKC_TRY(launch_gather_u32(s, F.cand, qidx, mq_ptr, m, qids));
   SKC_TRY(launch_gather_soa(s, ds->x, ds->n_pad, d, qids, mq_ptr, m, m_pad, xq));
   SKC_TRY(launch_gather_u4(s, cc, qidx, mq_ptr, m, qc));
+  SKC_TRY(launch_pad_q(s, mq_ptr, d, qc, xq, m_pad));
   SKC_TRY(launch_block_min(s, qc, mq_ptr, m, bmin));
 
   T.mark("cand: cells+q order");
@@ -443,7 +444,7 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   SKC_TRY(bitmap_tie_slab_words(d, ctx->num_sms, &slab_words));
   if (slab_words) SKC_TRY(A.alloc(&slab, slab_words));
   BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, boff, LT.unrank, K, LT.B, depth,
-                m_ptr, mq_ptr, work, (uint32_t)P.chunk, 0xffffffffu, dom, ext,
+                m_ptr, work, (uint32_t)P.chunk, 0xffffffffu, dom, ext,
                 P.blocks_per_sm * ctx->num_sms, slab};
   if (o.mode == SKC_MODE_BATCHED) {
     SKC_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), s));

@@ -56,6 +56,8 @@ int launch_gather_u32(cudaStream_t s, const uint32_t* in, const uint32_t* perm,
 int launch_member_flags(cudaStream_t s, const uint32_t* list, const uint32_t* m_ptr,
                         uint64_t m_max, const uint32_t* sorted_set, const uint32_t* nset_ptr,
                         uint8_t* st);
+int launch_pad_q(cudaStream_t s, const uint32_t* mq_ptr, int d, uint4* qc, float* qx,
+                 uint64_t pitch);
 int launch_sample_signature(cudaStream_t s, const float* x, uint64_t n_pad, uint64_t n, int d,
                             uint32_t* out);
 int launch_cap_count(cudaStream_t s, uint32_t* m_ptr, uint32_t cap, uint64_t* stats, int slot);
@@ -168,7 +170,7 @@ struct BitmapArgs {
   const uint4* pcells;   // candidate order
   const float* px;       // candidate order, attribute-major, pitch p_pad
   uint64_t p_pad;
-  const uint4* qcells;   // q order (level-sorted)
+  const uint4* qcells;   // q order (level-sorted), padded to whole 32-q blocks
   const float* qx;       // q order, attribute-major, pitch p_pad
   const uint4* bmin;     // per block of 32 q's
   const uint32_t* boff;  // q partitions: offsets in q order [K + 1]
@@ -177,7 +179,6 @@ struct BitmapArgs {
   int B;
   int depth;
   const uint32_t* m_ptr;   // candidates (p's)
-  const uint32_t* mq_ptr;  // q's (full-space skyline members, q order)
   uint32_t* work;        // work counter, must hold p_begin
   uint32_t chunk;        // candidates per work-counter grab (0: 1)
   uint32_t p_end;        // stop at min(m, p_end)

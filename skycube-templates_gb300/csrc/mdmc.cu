@@ -239,8 +239,7 @@ __global__ void __launch_bounds__(256) k_bitmaps(
     const float* __restrict__ qx, const uint4* __restrict__ bmin,
     const uint32_t* __restrict__ boff, const uint32_t* __restrict__ unrank,
     uint32_t K, int B, int depth,
-    const uint32_t* __restrict__ m_ptr, const uint32_t* __restrict__ mq_ptr,
-    uint32_t* __restrict__ work, uint32_t chunk,
+    const uint32_t* __restrict__ m_ptr, uint32_t* __restrict__ work, uint32_t chunk,
     uint32_t p_end_cap, uint32_t* __restrict__ out_dom,
     uint32_t* __restrict__ out_ext, uint32_t* __restrict__ tie_slab) {
   using BS = BitState<D>;
@@ -259,7 +258,6 @@ __global__ void __launch_bounds__(256) k_bitmaps(
                     ? wsm + (REG ? 0 : W)
                     : tie_slab + ((size_t)blockIdx.x * (blockDim.x / 32) + wib) * AW;
   const uint32_t m = *m_ptr;
-  const uint32_t mq = *mq_ptr;
   const uint32_t pend = min(m, p_end_cap);
   const uint32_t wi = REG ? (uint32_t)lane % W : 0;
   const int sh = depth - 1;
@@ -354,15 +352,15 @@ __global__ void __launch_bounds__(256) k_bitmaps(
           while (blocks) {
             const int bs = __ffs(blocks) - 1;
             blocks &= blocks - 1;
+            // The q arrays are padded to whole blocks with entries that add
+            // nothing (k_pad_q), so every lane of a block can be tested.
             const uint32_t qi = (k0 + bs) * 32 + lane;
-            const bool valid = qi < mq;
-            uint4 q4 = make_uint4(0, 0, 0, 0);
-            if (valid) q4 = qcells[qi];
+            const uint4 q4 = qcells[qi];
             uint32_t U = 0;
 #pragma unroll
             for (int w = 0; w < NW; ++w)
               U |= pack_guards(ge_bytes(pH[w], word_of(q4, w))) << (4 * w);
-            U = valid ? (U & (NSUB - 1)) : 0u;
+            U &= NSUB - 1;
             const bool hit = in_strict(U);
             if (__all_sync(kFull, hit)) continue;
 
@@ -548,7 +546,7 @@ static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
   if (a.grid_blocks > 0 && a.grid_blocks < grid) grid = a.grid_blocks;
   k_bitmaps<D><<<grid, 256, smem, s>>>(a.pcells, a.px, a.p_pad, a.qcells, a.qx,
                                         a.bmin, a.boff, a.unrank, a.K, a.B, a.depth,
-                                        a.m_ptr, a.mq_ptr, a.work, a.chunk ? a.chunk : 1u, a.p_end,
+                                        a.m_ptr, a.work, a.chunk ? a.chunk : 1u, a.p_end,
                                         a.out_dom, a.out_ext,
                                         a.tie_slab);
   SKC_LAUNCH_CHECK();

@@ -759,4 +759,26 @@ int launch_member_flags(cudaStream_t s, const uint32_t* list, const uint32_t* m_
   return SKC_OK;
 }
 
+// Pads the q list to a whole number of 32-q blocks with entries that add
+// nothing, so the bitmap kernel can test every lane of a block without a
+// bounds check: cells 127 (the top cell) and floats +inf. Such a q is worse
+// than p on every attribute where p's cell is below 127, and where p's cell
+// is 127 too the float test +inf <= p fails (inputs are finite), so LE = LT
+// = {} for every p: no strict update and no tie pair.
+__global__ void k_pad_q(const uint32_t* __restrict__ mq_ptr, int d, uint4* __restrict__ qc,
+                        float* __restrict__ qx, uint64_t pitch) {
+  const uint32_t mq = *mq_ptr;
+  const uint32_t i = mq + threadIdx.x;
+  if (i >= ((mq + 31) & ~31u)) return;
+  qc[i] = make_uint4(0x7f7f7f7fu, 0x7f7f7f7fu, 0x7f7f7f7fu, 0x7f7f7f7fu);
+  for (int k = 0; k < d; ++k) qx[(uint64_t)k * pitch + i] = __int_as_float(0x7f800000);
+}
+
+int launch_pad_q(cudaStream_t s, const uint32_t* mq_ptr, int d, uint4* qc, float* qx,
+                 uint64_t pitch) {
+  k_pad_q<<<1, 32, 0, s>>>(mq_ptr, d, qc, qx, pitch);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
 }  // namespace skc
