@@ -139,7 +139,19 @@ struct PartKernelArgs {
   uint8_t* status;          // list position -> status (zeroed, 4-byte padded)
   const uint32_t* splits;   // slices per work item of partition b [K]
   const uint32_t* cta_off;  // first CTA of partition b [K + 1]
+  uint32_t lvl_mul;         // strength level = cell sum * lvl_mul / lvl_span
+  uint32_t lvl_span;        //   (the sort's sub-key, k_mask_keys); 0: no cut
 };
+
+// Cell sum of compact cells over NA attributes (the sort's strength level
+// is sum * lvl_mul / lvl_span, k_mask_keys).
+template <int NA>
+__device__ __forceinline__ uint32_t cell_sum_na(const uint4& c) {
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < NA; ++k) sum += (word_of(c, k >> 2) >> (8 * (k & 3))) & 0x7fu;
+  return sum;
+}
 
 constexpr uint32_t kMaxSplits = 64;
 constexpr uint64_t kMinSliceWork = 256;  // q's (one tile): below this a slice is not worth a CTA
@@ -226,12 +238,16 @@ __global__ void __launch_bounds__(1024) k_split_plan(const uint32_t* __restrict_
 // dominated, 2 strictly dominated; 3 reads as strictly dominated). A sliced
 // partition neither publishes nor uses confirmed lists (no CTA knows its
 // points' final status); the others still do.
-template <int NA>
+//
+// LV (level cutoffs, used on unsliced lists): a thread stops scanning a
+// sorted partition at the first q above its own strength level.
+template <int NA, bool LV>
 __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
   constexpr int NW = (NA + 3) / 4;
   constexpr int TQ = 256;
   __shared__ uint4 q_cells[TQ];
   __shared__ float q_x[NA][TQ];
+  __shared__ uint16_t q_sum[LV ? TQ : 1];
   __shared__ uint32_t s_conf_end;
 
   __shared__ unsigned long long s_total;
@@ -277,6 +293,16 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
   uint8_t st = 0;
   bool done = !valid;
   bool all_done = false;
+  // Sort-filter bound: a q that dominates p, even weakly, has every cell
+  // <= p's, so its cell sum and strength level are <= p's. Inside a
+  // partition q's ascend in level, so a thread is finished with the
+  // partition at the first q above its own level. level(q) > level(p)
+  // exactly when cellsum(q) >= sum_cut, the smallest sum of a higher level.
+  uint32_t sum_cut = 0xffffffffu;  // no cut without strength levels
+  if (LV && a.lvl_mul) {
+    const uint32_t plv = cell_sum_na<NA>(my_cells) * a.lvl_mul / a.lvl_span;
+    sum_cut = ((plv + 1) * a.lvl_span + a.lvl_mul - 1) / a.lvl_mul;
+  }
   const uint32_t mb = a.unrank[b];
   const uint32_t s0 = a.sub_off[mb], s1 = a.sub_off[mb + 1];
   // This CTA's slice [s_lo, s_hi) of the concatenated submask partitions.
@@ -308,6 +334,7 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
       qend = qbeg + (uint32_t)(c1 - start);
       qbeg = qbeg + (uint32_t)(c0 - start);
     }
+    bool beyond = false;  // past this thread's level in this partition
     bool conf = false;
     if (use_conf && qb != b) {
       if (threadIdx.x == 0) {
@@ -327,28 +354,49 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
     }
     const uint4* qc = conf ? a.conf_cells : a.cells;
     const float* qxs = conf ? a.conf_x : a.xs;
+    bool first = true;
     for (uint32_t base = qbeg; base < qend; base += TQ) {
-      if (__syncthreads_and(done)) {
-        all_done = true;
+      // Without level cutoffs, or on a partition's first tile (nobody is
+      // beyond yet), the vote is "every point of the CTA is strictly
+      // dominated": the CTA is finished.
+      if (__syncthreads_and(done || (LV && beyond))) {
+        if (!LV || first) all_done = true;
         break;
       }
+      first = false;
       const uint32_t j = base + threadIdx.x;
       if (j < qend) {
         // Confirmed lists are written during this launch by other SMs: read
         // them through L2 (ld.cg), never from a possibly stale L1 line.
+        uint4 qcl;
         if (conf) {
-          q_cells[threadIdx.x] = __ldcg(qc + j);
+          qcl = __ldcg(qc + j);
 #pragma unroll
           for (int k = 0; k < NA; ++k) q_x[k][threadIdx.x] = __ldcg(qxs + (uint64_t)k * a.pitch + j);
         } else {
-          q_cells[threadIdx.x] = qc[j];
+          qcl = qc[j];
 #pragma unroll
           for (int k = 0; k < NA; ++k) q_x[k][threadIdx.x] = qxs[(uint64_t)k * a.pitch + j];
         }
+        q_cells[threadIdx.x] = qcl;
+        if constexpr (LV) q_sum[threadIdx.x] = (uint16_t)cell_sum_na<NA>(qcl);
       }
       __syncthreads();
-      if (!done) {
-        const uint32_t lim = min((uint32_t)TQ, qend - base);
+      if (!done && !(LV && beyond)) {
+        uint32_t lim = min((uint32_t)TQ, qend - base);
+        if (LV && !conf && sum_cut != 0xffffffffu) {
+          // First q of the tile above p's level (levels ascend in a sorted
+          // partition; confirmed lists are unordered and fully scanned).
+          uint32_t lo = 0, hi = lim;
+          while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (q_sum[mid] >= sum_cut) hi = mid; else lo = mid + 1;
+          }
+          if (lo < lim) {
+            lim = lo;
+            beyond = true;
+          }
+        }
         for (uint32_t t = 0; t < lim; ++t) {
           const uint4 q = q_cells[t];
           uint32_t worse = 0;  // guard bits where cell(q) > cell(p)
@@ -468,7 +516,12 @@ int launch_partition_skyline(cudaStream_t s, int d, int depth,
   SKC_LAUNCH_CHECK();
   PartKernelArgs k{ps.conf_cells, ps.conf_x, ps.ccount, ps.pdone, ps.sorted, ps.ccells, ps.cx,
                    pitch, ps.counts, ps.items, T.unrank, T.sub_off, T.sub_list, K, a.status,
-                   splits, cta_off};
+                   splits, cta_off,
+                   // Level cutoffs pay on lists full of dominated points (no
+                   // prefilter); on candidate-dense, sliced lists they only
+                   // cost (581k x 10 ties survivors: 3.05 -> 3.43 ms).
+                   a.split_target ? 0u : (1u << sub_bits) - 1u,
+                   ((1u << depth) - 1u) * (uint32_t)na};
   // Split CTAs OR their statuses in: start from zero (the buffer is padded
   // to a multiple of 4 bytes).
   SKC_CUDA(cudaMemsetAsync(a.status, 0, (a.m_max + 3) & ~3ull, s));
@@ -481,7 +534,10 @@ int launch_partition_skyline(cudaStream_t s, int d, int depth,
   const unsigned grid = (unsigned)((a.m_max + 255) / 256 + K + a.split_target);
 #define SKC_PART_CASE(N)                                  \
   case N:                                                 \
-    k_skyline_part<N><<<grid, 256, 0, s>>>(k);            \
+    if (k.lvl_mul)                                        \
+      k_skyline_part<N, true><<<grid, 256, 0, s>>>(k);    \
+    else                                                  \
+      k_skyline_part<N, false><<<grid, 256, 0, s>>>(k);   \
     break;
   switch (na) {
     SKC_PART_CASE(1) SKC_PART_CASE(2) SKC_PART_CASE(3) SKC_PART_CASE(4)
