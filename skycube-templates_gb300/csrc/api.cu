@@ -1624,6 +1624,38 @@ int skc_result_info(skc_result* r, int* d, uint64_t* n_cand, uint64_t* total) {
   return SKC_OK;
 }
 
+// Gives `v` at least n entries, from the context's pool of recycled host
+// buffers when one is large enough (its contents are overwritten by the
+// copy; entries past n are unused, views index through the offsets).
+static void take_host_buffer(skc_context* ctx, std::vector<uint32_t>& v, size_t n) {
+  if (v.size() >= n) return;
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto& pool = ctx->host_id_pool;
+    size_t best = pool.size();
+    for (size_t i = 0; i < pool.size(); ++i)
+      if (pool[i].size() >= n && (best == pool.size() || pool[i].size() < pool[best].size())) best = i;
+    if (best < pool.size()) {
+      v.swap(pool[best]);
+      pool.erase(pool.begin() + best);
+      return;
+    }
+  }
+  v.resize(n);
+}
+
+constexpr size_t kHostPoolBuffers = 4;
+
+// Returns a result's host id buffers to its context's pool.
+static void recycle_host_buffers(skc_context* ctx, skc_result* r) {
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  for (auto* v : {&r->h_ids, &r->h_eids}) {
+    if (v->empty()) continue;
+    if (ctx->host_id_pool.size() < kHostPoolBuffers) ctx->host_id_pool.push_back(std::move(*v));
+    v->clear();
+  }
+}
+
 static int download_csr(skc_result* r, bool ext) {
   bool& done = ext ? r->ext_downloaded : r->downloaded;
   if (done) return SKC_OK;
@@ -1639,7 +1671,7 @@ static int download_csr(skc_result* r, bool ext) {
   off.resize(nsub + 1);
   SKC_CUDA(cudaMemcpyAsync(off.data(), d_off, (nsub + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
   SKC_CUDA(cudaStreamSynchronize(s));
-  ids.resize(off[nsub]);
+  take_host_buffer(r->ctx, ids, off[nsub]);
   if (off[nsub])
     SKC_CUDA(cudaMemcpyAsync(ids.data(), d_ids, off[nsub] * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   SKC_CUDA(cudaStreamSynchronize(s));
@@ -1712,6 +1744,7 @@ int skc_result_free(skc_result* r) {
     skc_context* ctx = r->ctx;
     cudaStream_t s = r->stream ? r->stream : ctx->stream;
     cudaSetDevice(ctx->device);
+    recycle_host_buffers(ctx, r);
     release_result_memory(r);
     cudaStreamSynchronize(s);
   }

@@ -99,6 +99,10 @@ struct skc_context {
   std::set<skc_plan*> plans;
   // Per-phase device times of the last skc_skycube.
   std::vector<std::pair<std::string, float>> phases;
+  // Host id buffers of freed results, reused by later downloads: a fresh
+  // buffer costs its zero fill and first-touch page faults (about 3 ms for
+  // the 65 MB of a 1M x 10 skycube, eight times the copy itself).
+  std::vector<std::vector<uint32_t>> host_id_pool;
   // Work parameters chosen by skc_autotune, by signature key (api.cu).
   struct Tuned {
     int depth, pq_size, tile_points, chunk, blocks_per_sm;
