@@ -631,15 +631,27 @@ __global__ void __launch_bounds__(256) k_bits_count(
   const uint32_t t = blockIdx.x, w = blockIdx.y;
   const int lane = threadIdx.x & 31, k = threadIdx.x >> 5;
   const uint32_t m = *m_ptr;
+  // Cuboids of this word that are computed (all but the empty one without a
+  // cap; under -m a word may hold none): only their bit columns are counted.
+  const uint32_t wanted = __ballot_sync(kFull, cuboid_wanted(w * 32 + lane, nsub, max_d));
   uint32_t cnt = 0;
   const uint32_t row0 = t * kTileRows + k * 256;
-  if (t * kTileRows < m) {
+  if (t * kTileRows < m && wanted) {
+    const bool dense = __popc(wanted) > 16;  // then all 32 columns, unrolled
     for (int s = 0; s < 8; ++s) {
-      const uint32_t v = counted_bits(bits, W, row0 + s * 32 + lane, m, w, count_set);
+      const uint32_t v = counted_bits(bits, W, row0 + s * 32 + lane, m, w, count_set) & wanted;
+      if (dense) {
 #pragma unroll
-      for (int b = 0; b < 32; ++b) {
-        const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
-        if (lane == b) cnt += __popc(bal);
+        for (int b = 0; b < 32; ++b) {
+          const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
+          if (lane == b) cnt += __popc(bal);
+        }
+      } else {
+        for (uint32_t mm = wanted; mm; mm &= mm - 1) {
+          const int b = __ffs(mm) - 1;
+          const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
+          if (lane == b) cnt += __popc(bal);
+        }
       }
     }
   }
@@ -663,16 +675,26 @@ __global__ void __launch_bounds__(256) k_bits_write(
   const uint32_t t = blockIdx.x, w = blockIdx.y;
   const int lane = threadIdx.x & 31, k = threadIdx.x >> 5;
   const uint32_t m = *m_ptr;
-  if (t * kTileRows >= m) return;  // uniform over the CTA
+  const uint32_t wanted = __ballot_sync(kFull, cuboid_wanted(w * 32 + lane, nsub, max_d));
+  if (t * kTileRows >= m || !wanted) return;  // uniform over the CTA
   const uint32_t row0 = t * kTileRows + k * 256;
+  const bool dense = __popc(wanted) > 16;  // then all 32 columns, unrolled
   // pass 1: per-warp counts
   uint32_t cnt = 0;
   for (int s = 0; s < 8; ++s) {
-    const uint32_t v = counted_bits(bits, W, row0 + s * 32 + lane, m, w, count_set);
+    const uint32_t v = counted_bits(bits, W, row0 + s * 32 + lane, m, w, count_set) & wanted;
+    if (dense) {
 #pragma unroll
-    for (int b = 0; b < 32; ++b) {
-      const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
-      if (lane == b) cnt += __popc(bal);
+      for (int b = 0; b < 32; ++b) {
+        const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
+        if (lane == b) cnt += __popc(bal);
+      }
+    } else {
+      for (uint32_t mm = wanted; mm; mm &= mm - 1) {
+        const int b = __ffs(mm) - 1;
+        const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
+        if (lane == b) cnt += __popc(bal);
+      }
     }
   }
   wc[k][lane] = cnt;
@@ -691,14 +713,16 @@ __global__ void __launch_bounds__(256) k_bits_write(
   const uint32_t lt_mask = (1u << lane) - 1u;
   for (int s = 0; s < 8; ++s) {
     const uint32_t r = row0 + s * 32 + lane;
-    const uint32_t v = counted_bits(bits, W, r, m, w, count_set);
+    const uint32_t v = counted_bits(bits, W, r, m, w, count_set) & wanted;
     const uint32_t id = r < m ? cand[r] : 0u;
+    // Dense words walk all 32 columns (unwanted ones are masked to zero).
+    const uint32_t cols = dense ? kFull : wanted;
 #pragma unroll 4
-    for (int b = 0; b < 32; ++b) {
+    for (uint32_t mm = cols; mm; mm &= mm - 1) {
+      const int b = __ffs(mm) - 1;
       const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
       if (!bal) continue;
       const uint32_t c = w * 32 + b;
-      if (!cuboid_wanted(c, nsub, max_d)) continue;
       const uint32_t base = run[k][b];
       if ((v >> b) & 1u) {
         const uint64_t pos = offs[(uint64_t)c * T + t] + base + __popc(bal & lt_mask);
