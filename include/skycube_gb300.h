@@ -90,7 +90,10 @@ typedef struct skc_options {
                         skyline (-q; Config::pq_size, src/utilities/config.h:20):
                         > 0 that many, applied when n > 2 * pq_size as the
                         suite does (src/mdmc/MDMC.cu:251); < 0 off; 0 auto
-                        (default 128 when n >= 32768) */
+                        (default 512 when n >= 32768). Applied in two
+                        passes: the strongest pq_size / 16 on every point,
+                        the rest on the survivors when at least a quarter
+                        of the points survive */
   int tile_points;   /* bitmap kernel: mean q points per median partition
                         (a power of two, 32..65536); 0 auto (256) */
   int chunk;         /* bitmap kernel: candidates a warp takes per work-queue

@@ -280,6 +280,8 @@ static int run_full_space(Exec& E, skc_dataset* ds, const RunParams& P, Arena& A
     SKC_TRY(A.alloc(&pf.st, n));
     SKC_TRY(A.alloc(&pf.blk0, nb));
     SKC_TRY(A.alloc(&pf.blk1, nb));
+    SKC_TRY(A.alloc(&pf.mid_ids, n));
+    SKC_TRY(A.alloc(&pf.mid_count, 1));
     uint32_t *surv, *d_ns;
     SKC_TRY(A.alloc(&surv, n));
     SKC_TRY(A.alloc(&d_ns, 1));
@@ -668,7 +670,10 @@ static int auto_depth(uint64_t n, int d) {
 
 // Defaults of the work parameters (used when neither the options nor a
 // stored tuning set them).
-constexpr int kDefaultPruners = 128;             // the suite's -q default
+// Pruners: 512 in two passes (32 on every point, the rest on the survivors
+// when at least a quarter survive; prefilter.cu). The suite's -q default is
+// 128 (one pass).
+constexpr int kDefaultPruners = 512;
 constexpr uint64_t kPrefilterMinPoints = 32768;  // below: launch-bound anyway
 constexpr int kDefaultTilePoints = 256;
 
@@ -1114,6 +1119,8 @@ static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, const RunPara
       SKC_TRY(A.alloc(&pf.st, m));
       SKC_TRY(A.alloc(&pf.blk0, nblk));
       SKC_TRY(A.alloc(&pf.blk1, nblk));
+      SKC_TRY(A.alloc(&pf.mid_ids, m));
+      SKC_TRY(A.alloc(&pf.mid_count, 1));
       uint32_t *surv, *d_ns;
       SKC_TRY(A.alloc(&surv, m));
       SKC_TRY(A.alloc(&d_ns, 1));

@@ -148,6 +148,8 @@ struct PrefilterScratch {
   uint8_t* st;         // [m_max]
   uint32_t* blk0;      // [m_max / 1024 + 1]
   uint32_t* blk1;      // [m_max / 1024 + 1]
+  uint32_t* mid_ids;   // [m_max] survivors of the first pass
+  uint32_t* mid_count; // [1]
 };
 struct PrefilterArgs {
   const uint4* cells;    // point id -> grid cells

@@ -170,7 +170,9 @@ __global__ void __launch_bounds__(1024) k_pruner_order(const uint32_t* __restric
   }
 }
 
-// st[i] = 2 when a pruner strictly dominates list entry i on S, else 0.
+// st[i] = 2 when one of the pruners of rank [r0, r1) strictly dominates
+// list entry i on S, else 0. With gate_m set, the pass runs only when the
+// list holds at least *gate_m / 4 entries (otherwise every entry is kept).
 template <int D>
 __global__ void __launch_bounds__(256) k_prefilter(const uint4* __restrict__ cells,
                                                    const float* __restrict__ x, uint64_t n_pad,
@@ -179,22 +181,30 @@ __global__ void __launch_bounds__(256) k_prefilter(const uint4* __restrict__ cel
                                                    const uint32_t* __restrict__ sel,
                                                    const uint4* __restrict__ pr_cells,
                                                    const float* __restrict__ pr_x, uint32_t K,
+                                                   uint32_t r0, uint32_t r1,
+                                                   const uint32_t* __restrict__ gate_m,
                                                    uint8_t* __restrict__ st) {
   constexpr int NW = (D + 3) / 4;
   extern __shared__ uint4 sm4[];
-  uint4* s_cells = sm4;                            // [K]
-  float* s_x = reinterpret_cast<float*>(sm4 + K);  // [D][K]
-  const uint32_t Kp = sel[2];
+  const uint32_t R = r1 - r0;                      // smem rows
+  uint4* s_cells = sm4;                            // [R]
+  float* s_x = reinterpret_cast<float*>(sm4 + R);  // [D][R]
+  const uint32_t m = *m_ptr;
+  if (gate_m && 4ull * m < *gate_m) {  // few survivors: this pass would not pay
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+      st[i] = 0;
+    return;
+  }
+  const uint32_t Kp = min(sel[2], r1) > r0 ? min(sel[2], r1) - r0 : 0u;
   for (uint32_t t = threadIdx.x; t < Kp; t += blockDim.x) {
-    s_cells[t] = pr_cells[t];
+    s_cells[t] = pr_cells[r0 + t];
 #pragma unroll
-    for (int k = 0; k < D; ++k) s_x[k * K + t] = pr_x[(uint64_t)k * K + t];
+    for (int k = 0; k < D; ++k) s_x[k * R + t] = pr_x[(uint64_t)k * K + r0 + t];
   }
   __syncthreads();
   uint32_t hS[NW];
 #pragma unroll
   for (int w = 0; w < NW; ++w) hS[w] = guard_mask(S, w);
-  const uint32_t m = *m_ptr;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
     const uint32_t id = ids ? ids[i] : i;
     const uint4 c4 = cells[id];
@@ -221,7 +231,7 @@ __global__ void __launch_bounds__(256) k_prefilter(const uint4* __restrict__ cel
       bool strict = true;
 #pragma unroll
       for (int k = 0; k < D; ++k)
-        if ((Z >> k) & 1u) strict &= s_x[k * K + t] < pv[k];
+        if ((Z >> k) & 1u) strict &= s_x[k * R + t] < pv[k];
       pruned = strict;
     }
     st[i] = pruned ? 2 : 0;
@@ -233,15 +243,32 @@ size_t prefilter_smem(int d, uint32_t K) {
 }
 
 template <int D>
-static int launch_prefilter_d(cudaStream_t s, const PrefilterArgs& a, unsigned grid) {
-  const size_t smem = prefilter_smem(D, a.K);
+static int launch_prefilter_d(cudaStream_t s, const PrefilterArgs& a, unsigned grid,
+                              const uint32_t* ids, const uint32_t* m_ptr, uint32_t r0,
+                              uint32_t r1, const uint32_t* gate_m) {
+  const size_t smem = prefilter_smem(D, r1 - r0);
   if (smem > 48 * 1024)
     SKC_CUDA(cudaFuncSetAttribute(k_prefilter<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
-  k_prefilter<D><<<grid, 256, smem, s>>>(a.cells, a.x, a.n_pad, a.ids, a.m_ptr, a.S,
-                                         a.ps.sel, a.ps.pr_cells, a.ps.pr_x, a.K, a.ps.st);
+  k_prefilter<D><<<grid, 256, smem, s>>>(a.cells, a.x, a.n_pad, ids, m_ptr, a.S, a.ps.sel,
+                                         a.ps.pr_cells, a.ps.pr_x, a.K, r0, r1, gate_m, a.ps.st);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
+}
+
+static int launch_prefilter_pass(cudaStream_t s, int d, const PrefilterArgs& a, unsigned grid,
+                                 const uint32_t* ids, const uint32_t* m_ptr, uint32_t r0,
+                                 uint32_t r1, const uint32_t* gate_m) {
+  switch (d) {
+#define SKC_PF_CASE(D) \
+  case D: return launch_prefilter_d<D>(s, a, grid, ids, m_ptr, r0, r1, gate_m);
+    SKC_PF_CASE(2) SKC_PF_CASE(3) SKC_PF_CASE(4) SKC_PF_CASE(5) SKC_PF_CASE(6)
+    SKC_PF_CASE(7) SKC_PF_CASE(8) SKC_PF_CASE(9) SKC_PF_CASE(10) SKC_PF_CASE(11)
+    SKC_PF_CASE(12) SKC_PF_CASE(13) SKC_PF_CASE(14) SKC_PF_CASE(15) SKC_PF_CASE(16)
+#undef SKC_PF_CASE
+    default:
+      return set_error(SKC_ERR_INVALID, "unsupported d=%d", d);
+  }
 }
 
 int launch_prefilter(cudaStream_t s, int d, int num_sms, const PrefilterArgs& a,
@@ -263,19 +290,24 @@ int launch_prefilter(cudaStream_t s, int d, int num_sms, const PrefilterArgs& a,
   k_pruner_order<<<1, 1024, 0, s>>>(p.pr_ids, p.pr_key, p.sel, a.cells, a.x, a.n_pad, d, a.K,
                                     p.pr_cells, p.pr_x);
   SKC_LAUNCH_CHECK();
-  switch (d) {
-#define SKC_PF_CASE(D) \
-  case D: SKC_TRY(launch_prefilter_d<D>(s, a, grid)); break;
-    SKC_PF_CASE(2) SKC_PF_CASE(3) SKC_PF_CASE(4) SKC_PF_CASE(5) SKC_PF_CASE(6)
-    SKC_PF_CASE(7) SKC_PF_CASE(8) SKC_PF_CASE(9) SKC_PF_CASE(10) SKC_PF_CASE(11)
-    SKC_PF_CASE(12) SKC_PF_CASE(13) SKC_PF_CASE(14) SKC_PF_CASE(15) SKC_PF_CASE(16)
-#undef SKC_PF_CASE
-    default:
-      return set_error(SKC_ERR_INVALID, "unsupported d=%d", d);
+  // Two passes: the strongest K1 = K / 16 pruners on every entry, then, only
+  // when at least a quarter of the entries survived, the other pruners on
+  // the survivors. Tie-heavy and correlated data lose nearly everything to
+  // the first pass (more pruners only cost there: survivors that nothing can
+  // strictly dominate walk every pruner); anticorrelated data keeps most
+  // points, and the second pass removes a good part of them.
+  const uint32_t K1 = std::max<uint32_t>(1, a.K / 16);
+  SKC_TRY(launch_prefilter_pass(s, d, a, grid, a.ids, a.m_ptr, 0, K1, nullptr));
+  if (K1 >= a.K) {
+    return launch_status_compact(s, p.st, a.ids, a.m_ptr, a.m_max, 1, p.blk0, p.blk1, out_ids,
+                                 nullptr, out_count, nullptr);
   }
+  SKC_TRY(launch_status_compact(s, p.st, a.ids, a.m_ptr, a.m_max, 1, p.blk0, p.blk1, p.mid_ids,
+                                nullptr, p.mid_count, nullptr));
+  SKC_TRY(launch_prefilter_pass(s, d, a, grid, p.mid_ids, p.mid_count, K1, a.K, a.m_ptr));
   // Survivors (status 0) in list order, as point ids.
-  return launch_status_compact(s, p.st, a.ids, a.m_ptr, a.m_max, 1, p.blk0, p.blk1, out_ids,
-                               nullptr, out_count, nullptr);
+  return launch_status_compact(s, p.st, p.mid_ids, p.mid_count, a.m_max, 1, p.blk0, p.blk1,
+                               out_ids, nullptr, out_count, nullptr);
 }
 
 uint32_t prefilter_sum_bins() { return kSumBins; }
