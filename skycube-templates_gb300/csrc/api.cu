@@ -384,11 +384,11 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   uint32_t *qpos, *mq_ptr;
   SKC_TRY(A.alloc(&qpos, m));
   SKC_TRY(A.alloc(&mq_ptr, 1));
+  uint8_t* qst;  // per candidate: 0 full-space skyline, 2 dominated there
+  SKC_TRY(A.alloc(&qst, m));
   {
     const uint64_t nb = (m + 1023) / 1024 + 1;
-    uint8_t* qst;
     uint32_t *b0, *b1;
-    SKC_TRY(A.alloc(&qst, m));
     SKC_TRY(A.alloc(&b0, nb));
     SKC_TRY(A.alloc(&b1, nb));
     SKC_TRY(launch_member_flags(s, F.cand, m_ptr, m, F.sky, F.counts + 0, qst));
@@ -448,6 +448,13 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, boff, LT.unrank, K, LT.B, depth,
                 m_ptr, work, (uint32_t)P.chunk, 0xffffffffu, dom, ext,
                 P.blocks_per_sm * ctx->num_sms, slab};
+  // A cap below d - 1 lets the kernel skip q's that only reach subspaces
+  // above it; the bits there are then not computed, so per-point bitmaps
+  // (want_bitmaps) keep the full computation.
+  if (max_d <= d - 2 && !o.want_bitmaps) {
+    ba.cap = max_d;
+    ba.full_dom = qst;
+  }
   if (o.mode == SKC_MODE_BATCHED) {
     SKC_CUDA(cudaMemsetAsync(work, 0, sizeof(uint32_t), s));
     SKC_TRY(launch_bitmaps(s, d, ctx->num_sms, ba));

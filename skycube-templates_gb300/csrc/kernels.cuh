@@ -188,6 +188,12 @@ struct BitmapArgs {
   uint32_t* out_ext;     // [m][words] extended-skyline bitmaps, or nullptr
   int grid_blocks;       // persistent grid (0: from occupancy)
   uint32_t* tie_slab;    // global tie maps (bitmap_tie_slab_words), or nullptr
+  // Capped skycubes: only the bits of subspaces with at most `cap`
+  // attributes and of the full space are exact (1 <= cap <= d - 2; 0: all
+  // bits). The full-space bits then come from full_dom (per candidate,
+  // nonzero when it is dominated on the full space).
+  int cap = 0;
+  const uint8_t* full_dom = nullptr;
 };
 int launch_bitmaps(cudaStream_t s, int d, int num_sms, const BitmapArgs& a);
 int bitmap_tie_slab_words(int d, int num_sms, uint64_t* words);

@@ -35,6 +35,8 @@ namespace skc {
 
 // c_submask[x] = bit b set iff b is a subset of x (5-bit masks).
 __constant__ uint32_t c_submask[32];
+// c_popabove[c] = bit b set iff b has more than c set bits (c = 0 .. 4).
+__constant__ uint32_t c_popabove[5];
 
 void upload_submask_table() {
   uint32_t t[32];
@@ -45,6 +47,14 @@ void upload_submask_table() {
     t[x] = m;
   }
   cudaMemcpyToSymbol(c_submask, t, sizeof(t));
+  uint32_t a[5];
+  for (int c = 0; c < 5; ++c) {
+    uint32_t m = 0;
+    for (uint32_t b = 0; b < 32; ++b)
+      if (__builtin_popcount(b) > c) m |= 1u << b;
+    a[c] = m;
+  }
+  cudaMemcpyToSymbol(c_popabove, a, sizeof(a));
 }
 
 constexpr uint32_t kFull = 0xffffffffu;
@@ -159,6 +169,18 @@ __device__ __forceinline__ uint32_t spread_even(uint32_t x) {
   return x;
 }
 
+// Output word t with the full-space bit (word W - 1) replaced, capped mode.
+struct FullFix {
+  uint32_t word = 0xffffffffu;  // no word
+  uint32_t set = 0, clr = 0;
+  __device__ __forceinline__ void apply(uint32_t t, uint32_t& dom, uint32_t& ext) const {
+    if (t == word) {
+      dom = (dom & ~clr) | set;
+      ext = (ext & ~clr) | set;
+    }
+  }
+};
+
 // Phase 2, per chunk: load it into the scratch Cs, close its ten low entry
 // bits there, and turn it straight into the chunk's 32 output words (entry
 // S is tie-dominated iff S meets T[S]): word j of the chunk gives the bits
@@ -168,7 +190,7 @@ __device__ __forceinline__ uint32_t spread_even(uint32_t x) {
 template <int D>
 __device__ void tie_global_output(uint32_t* A, uint32_t* Cs, const uint32_t* sat_s, int lane,
                                   uint32_t p, uint32_t* __restrict__ out_dom,
-                                  uint32_t* __restrict__ out_ext) {
+                                  uint32_t* __restrict__ out_ext, const FullFix& fix) {
   constexpr int HB = D - 10;
   constexpr uint32_t NC = 1u << HB;
   constexpr uint32_t W = (1u << D) / 32;
@@ -211,6 +233,7 @@ __device__ void tie_global_output(uint32_t* A, uint32_t* Cs, const uint32_t* sat
       dom &= ~1u;
       ext &= ~1u;
     }
+    fix.apply(t, dom, ext);
     out_dom[(uint64_t)p * W + t] = dom;
     if (out_ext) out_ext[(uint64_t)p * W + t] = ext;
     __syncwarp();  // Cs is reused by the next chunk
@@ -232,7 +255,70 @@ __device__ __forceinline__ uint32_t tie_word(const uint32_t* A, uint32_t t) {
   return bits;
 }
 
+// Capped skycubes (only cuboids of at most `cap` attributes and the full
+// space are output). A q whose U has every subspace of at most `cap`
+// attributes in STRICT changes no output bit below the cap, so the
+// membership test may use the larger down-closed set
+//   NR = {U : every S subset of U with |S| <= cap is in STRICT}
+// instead of STRICT. The bitmap then holds STRICT on the levels <= cap and
+// a subset of NR above (the updates keep it so); a closure turns the levels
+// above the cap into exactly NR: set them to 1, then AND every entry with
+// its subsets, one attribute at a time. The full-space bit is not derived
+// from the q's in this mode; it is the candidate's known full-space status.
+__device__ __forceinline__ uint32_t pop_above(int c) {
+  return c < 0 ? kFull : (c >= 5 ? 0u : c_popabove[c]);
+}
+
+// Entries b of a word (5-bit masks): b &= b minus each of its bits.
+__device__ __forceinline__ uint32_t subset_and_in_word(uint32_t x) {
+  x &= (x << 1) | 0x55555555u;
+  x &= (x << 2) | 0x33333333u;
+  x &= (x << 4) | 0x0f0f0f0fu;
+  x &= (x << 8) | 0x00ff00ffu;
+  x &= (x << 16) | 0x0000ffffu;
+  return x;
+}
+
+// Registers (d <= 10): lane holds word wi (W words, W a power of two).
 template <int D>
+__device__ __forceinline__ uint32_t nr_close_reg(uint32_t x, uint32_t wi, int cap) {
+  constexpr uint32_t W = BitState<D>::W;
+  x = subset_and_in_word(x | pop_above(cap - __popc(wi)));
+#pragma unroll
+  for (int j = 0; (1u << j) < W; ++j) {
+    const uint32_t y = __shfl_xor_sync(kFull, x, 1 << j);
+    if (wi & (1u << j)) x &= y;
+  }
+  return x;
+}
+
+// Shared memory (d >= 11): lane owns words 32i + lane. Word bits 0..4 are
+// exchanged by shuffles, the row bits i stay inside the lane's column.
+template <int D>
+__device__ void nr_close_smem(uint32_t* sat_s, int lane, int cap) {
+  constexpr uint32_t R = BitState<D>::W / 32;
+  __syncwarp();
+  for (uint32_t i = 0; i < R; ++i) {
+    const uint32_t w = 32 * i + lane;
+    uint32_t x = subset_and_in_word(sat_s[w] | pop_above(cap - __popc(w)));
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      const uint32_t y = __shfl_xor_sync(kFull, x, 1 << j);
+      if (lane & (1 << j)) x &= y;
+    }
+    sat_s[w] = x;
+  }
+  for (uint32_t j = 0; (1u << j) < R; ++j) {
+    const uint32_t st = 1u << j;
+    for (uint32_t t = 0; t < R / 2; ++t) {
+      const uint32_t i = ((t >> j) << (j + 1)) | st | (t & (st - 1));
+      sat_s[32 * i + lane] &= sat_s[32 * (i ^ st) + lane];
+    }
+  }
+  __syncwarp();
+}
+
+template <int D, bool CAP>
 __global__ void __launch_bounds__(256) k_bitmaps(
     const uint4* __restrict__ pcells, const float* __restrict__ px,
     uint64_t p_pad, const uint4* __restrict__ qcells,
@@ -241,7 +327,8 @@ __global__ void __launch_bounds__(256) k_bitmaps(
     uint32_t K, int B, int depth,
     const uint32_t* __restrict__ m_ptr, uint32_t* __restrict__ work, uint32_t chunk,
     uint32_t p_end_cap, uint32_t* __restrict__ out_dom,
-    uint32_t* __restrict__ out_ext, uint32_t* __restrict__ tie_slab) {
+    uint32_t* __restrict__ out_ext, uint32_t* __restrict__ tie_slab, int cap,
+    const uint8_t* __restrict__ full_dom) {
   using BS = BitState<D>;
   constexpr int NW = (D + 3) / 4;
   constexpr uint32_t NSUB = BS::NSUB;
@@ -261,6 +348,9 @@ __global__ void __launch_bounds__(256) k_bitmaps(
   const uint32_t pend = min(m, p_end_cap);
   const uint32_t wi = REG ? (uint32_t)lane % W : 0;
   const int sh = depth - 1;
+  // Capped mode, d >= 11: blocks walked between closures (a closure costs
+  // about as much as walking W / 32 blocks).
+  constexpr uint32_t kCloseBlocks = W / 32;
 
   for (;;) {
     // The warp takes `chunk` consecutive candidates per grab.
@@ -295,6 +385,24 @@ __global__ void __launch_bounds__(256) k_bitmaps(
       for (uint32_t w = lane; w < W; w += 32) sat_s[w] = (w == 0) ? 1u : 0u;
       __syncwarp();
     }
+    FullFix fix;
+    bool dirty = false;   // capped: STRICT grew since the last closure
+    uint32_t since = 0;   // capped, d >= 11: blocks walked since then
+    if constexpr (CAP) {
+      fix.word = W - 1;
+      const uint32_t fb = 1u << ((NSUB - 1) & 31);
+      if (full_dom[p]) fix.set = fb; else fix.clr = fb;
+    }
+    // Capped, d >= 11: close when STRICT grew and enough blocks were walked.
+    auto maybe_close = [&]() {
+      if constexpr (CAP && !REG) {
+        if (dirty && since >= kCloseBlocks) {
+          nr_close_smem<D>(sat_s, lane, cap);
+          dirty = false;
+          since = 0;
+        }
+      }
+    };
     bool touched = false;  // tie map in use for this p
     // d >= 13: 0 no tie pair, 1 pairs in the list, 2 pairs in the global map
     int tmode = 0;
@@ -312,6 +420,10 @@ __global__ void __launch_bounds__(256) k_bitmaps(
     // (all but those where the partition is above the median and p is not)
     // already form a strictly dominated subspace.
     for (uint32_t b0 = 0; b0 < K; b0 += 32) {
+      maybe_close();
+      if constexpr (CAP) {  // every subspace within the cap is strict
+        if (in_strict(NSUB - 1)) break;
+      }
       const uint32_t bl = b0 + lane;
       uint32_t qbeg_l = 0, qend_l = 0, Sb = 0;
       if (bl < K) {
@@ -326,6 +438,9 @@ __global__ void __launch_bounds__(256) k_bitmaps(
       while (parts) {
         const int ps = __ffs(parts) - 1;
         parts &= parts - 1;
+        if constexpr (CAP) {  // the set may have grown since the ballot
+          if (in_strict(__shfl_sync(kFull, Sb, ps))) continue;
+        }
         const uint32_t qbeg = __shfl_sync(kFull, qbeg_l, ps);
         const uint32_t qend = __shfl_sync(kFull, qend_l, ps);
         // A block shared with the previous partition is visited once; its
@@ -337,6 +452,7 @@ __global__ void __launch_bounds__(256) k_bitmaps(
         // Blocks are tested 32 at a time against their byte-wise minimum
         // cells, then the surviving blocks are walked one by one.
         for (uint32_t k0 = blk_first; k0 < blk_end; k0 += 32) {
+          maybe_close();
           const uint32_t kb = k0 + lane;
           uint32_t Ub = 0;
           if (kb < blk_end) {
@@ -349,9 +465,13 @@ __global__ void __launch_bounds__(256) k_bitmaps(
           const bool ub_strict = in_strict(Ub);  // every lane (shuffle)
           const bool blk_skip = (kb >= blk_end) || ub_strict;
           uint32_t blocks = __ballot_sync(kFull, !blk_skip);
+          if constexpr (CAP && !REG) since += 1 + __popc(blocks);
           while (blocks) {
             const int bs = __ffs(blocks) - 1;
             blocks &= blocks - 1;
+            if constexpr (CAP && REG) {  // closed after every update
+              if (in_strict(__shfl_sync(kFull, Ub, bs))) continue;
+            }
             // The q arrays are padded to whole blocks with entries that add
             // nothing (k_pad_q), so every lane of a block can be tested.
             const uint32_t qi = (k0 + bs) * 32 + lane;
@@ -431,6 +551,7 @@ __global__ void __launch_bounds__(256) k_bitmaps(
               todo &= todo - 1;
               const uint32_t L = __shfl_sync(kFull, lt, src);
               if (in_strict(L)) continue;  // covered by an earlier update
+              if constexpr (CAP) dirty = true;
               if (REG) {
                 if ((wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
               } else {
@@ -449,6 +570,12 @@ __global__ void __launch_bounds__(256) k_bitmaps(
                 __syncwarp();
               }
             }
+            if constexpr (CAP && REG) {
+              if (dirty) {
+                sat = nr_close_reg<D>(sat, wi, cap);
+                dirty = false;
+              }
+            }
           }
         }
       }
@@ -459,7 +586,7 @@ __global__ void __launch_bounds__(256) k_bitmaps(
     if constexpr (!BS::A_SMEM) {
       if (tmode == 2) {
         __syncwarp();
-        tie_global_output<D>(A, wsm + W, sat_s, lane, p, out_dom, out_ext);
+        tie_global_output<D>(A, wsm + W, sat_s, lane, p, out_dom, out_ext, fix);
         __syncwarp();
         continue;
       }
@@ -482,6 +609,7 @@ __global__ void __launch_bounds__(256) k_bitmaps(
             dom &= ~1u;
             ext &= ~1u;
           }
+          if constexpr (CAP) fix.apply(w, dom, ext);
           out_dom[(uint64_t)p * W + w] = dom;
           if (out_ext) out_ext[(uint64_t)p * W + w] = ext;
         }
@@ -502,6 +630,7 @@ __global__ void __launch_bounds__(256) k_bitmaps(
           dom &= ~1u;
           ext &= ~1u;
         }
+        if constexpr (CAP) fix.apply(lane, dom, ext);
         out_dom[(uint64_t)p * W + lane] = dom;
         if (out_ext) out_ext[(uint64_t)p * W + lane] = ext;
       }
@@ -514,6 +643,7 @@ __global__ void __launch_bounds__(256) k_bitmaps(
           dom &= ~1u;
           ext &= ~1u;
         }
+        if constexpr (CAP) fix.apply(w, dom, ext);
         out_dom[(uint64_t)p * W + w] = dom;
         if (out_ext) out_ext[(uint64_t)p * W + w] = ext;
       }
@@ -523,34 +653,62 @@ __global__ void __launch_bounds__(256) k_bitmaps(
   }
 }
 
-template <int D>
-static int bitmap_grid_d(int num_sms, int* grid, size_t* smem) {
+// Capped kernels exist for d >= 6 (below, a cap under d - 1 leaves too few
+// cuboids to matter and the uncapped kernel serves).
+constexpr int kMinCapDims = 6;
+
+template <int D, bool CAP>
+static int bitmap_grid_dc(int num_sms, int* grid, size_t* smem) {
   using BS = BitState<D>;
   constexpr int threads = 256;
   *smem = (size_t)(threads / 32) * BS::SMEM_WORDS * sizeof(uint32_t);
   if (*smem > 48 * 1024)
-    SKC_CUDA(cudaFuncSetAttribute(k_bitmaps<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem));
+    SKC_CUDA(cudaFuncSetAttribute(k_bitmaps<D, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem));
   int per_sm = 0;
-  SKC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmaps<D>, threads, *smem));
+  SKC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bitmaps<D, CAP>, threads, *smem));
   if (per_sm < 1) per_sm = 1;
   if (!BS::A_SMEM && per_sm > 4) per_sm = 4;  // bounds the global tie-map slab
   *grid = per_sm * num_sms;
   return SKC_OK;
 }
 
+// Persistent grid of the bitmap kernel: the larger of the two variants' (the
+// tie-map slab is sized by it).
 template <int D>
-static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
+static int bitmap_grid_d(int num_sms, int* grid, size_t* smem) {
+  SKC_TRY((bitmap_grid_dc<D, false>(num_sms, grid, smem)));
+  if constexpr (D >= kMinCapDims) {
+    int g2 = 0;
+    size_t s2 = 0;
+    SKC_TRY((bitmap_grid_dc<D, true>(num_sms, &g2, &s2)));
+    if (g2 > *grid) *grid = g2;
+  }
+  return SKC_OK;
+}
+
+template <int D, bool CAP>
+static int launch_bitmaps_dc(cudaStream_t s, int num_sms, const BitmapArgs& a) {
   int grid = 0;
   size_t smem = 0;
-  SKC_TRY(bitmap_grid_d<D>(num_sms, &grid, &smem));
+  SKC_TRY((bitmap_grid_dc<D, CAP>(num_sms, &grid, &smem)));
   if (a.grid_blocks > 0 && a.grid_blocks < grid) grid = a.grid_blocks;
-  k_bitmaps<D><<<grid, 256, smem, s>>>(a.pcells, a.px, a.p_pad, a.qcells, a.qx,
-                                        a.bmin, a.boff, a.unrank, a.K, a.B, a.depth,
-                                        a.m_ptr, a.work, a.chunk ? a.chunk : 1u, a.p_end,
-                                        a.out_dom, a.out_ext,
-                                        a.tie_slab);
+  k_bitmaps<D, CAP><<<grid, 256, smem, s>>>(a.pcells, a.px, a.p_pad, a.qcells, a.qx,
+                                             a.bmin, a.boff, a.unrank, a.K, a.B, a.depth,
+                                             a.m_ptr, a.work, a.chunk ? a.chunk : 1u, a.p_end,
+                                             a.out_dom, a.out_ext,
+                                             a.tie_slab, a.cap, a.full_dom);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
+}
+
+template <int D>
+static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
+  if (a.cap > 0) {
+    if (a.cap > D - 2 || !a.full_dom)
+      return set_error(SKC_ERR_INVALID, "bitmap cap %d needs 1 <= cap <= d - 2 and full-space flags", a.cap);
+    if constexpr (D >= kMinCapDims) return launch_bitmaps_dc<D, true>(s, num_sms, a);
+  }
+  return launch_bitmaps_dc<D, false>(s, num_sms, a);
 }
 
 #define SKC_BITMAP_DISPATCH(fn, ...)                    \
