@@ -15,6 +15,8 @@ form (MDMC bitmaps, one launch for every cuboid). The JSON line reports:
              issue roofline (pair-test lane operations / SM lane-op peak)
   cpu_baseline  the CPU oracle (restated STSC, all host threads) on a bounded
              sample of the same workload
+  reference_sweeps  capped skycubes of 500k x 16 points at the caps of the
+             reference's published sweeps, beside its published milliseconds
 
 --impl reference times the reference's CPU path (the restated STSC oracle;
 the reference's own build is x86-only) on a bounded sample of the same
@@ -52,6 +54,8 @@ def parse_args():
     ap.add_argument("--no-plain", action="store_true", help="skip the per-cuboid form")
     ap.add_argument("--cpu-sample", type=int, default=0, help="points in the CPU sample (0: auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-sweeps", action="store_true",
+                    help="skip the reference's published sweep workloads")
     ap.add_argument("--serving-queries", type=int, default=600,
                     help="queries of the serving stream (0: skip serving)")
     ap.add_argument("--serving-rate", type=float, default=40.0, help="Poisson arrival rate, queries/s")
@@ -248,6 +252,61 @@ def run_serving(sk, ctx, args):
     return out
 
 
+# The reference's only published timings: its authors' sweep scripts, SDSC on
+# one GPU (CUDA 8 era, GPU model not stated) over 500k-point 16-d synthetic
+# files, Execute() wall ms per cap -m (Release/scaleanticorr16:29-35,
+# Release/scalecorrelated16:15-21).
+REFERENCE_SWEEPS = [
+    ("anticorrelated", 4, 25469.0, "Release/scaleanticorr16:29"),
+    ("anticorrelated", 6, 279723.0, "Release/scaleanticorr16:30"),
+    ("anticorrelated", 8, 1109848.0, "Release/scaleanticorr16:31"),
+    ("correlated", 4, 9487.0, "Release/scalecorrelated16:15"),
+    ("correlated", 6, 74686.0, "Release/scalecorrelated16:16"),
+    ("correlated", 8, 240978.0, "Release/scalecorrelated16:17"),
+    ("correlated", 10, 422859.0, "Release/scalecorrelated16:18"),
+]
+
+
+def run_reference_sweeps(sk, ctx):
+    """Capped skycubes of 500,000 x 16 points (seeded stand-ins for the
+    authors' anticorrelated and correlated files, which are not shipped) at
+    the caps of the reference's published sweeps, batched form. device_ms:
+    CUDA events around the skycube call, dataset resident (best of two after
+    a warm-up). e2e_ms: host rows in, every cuboid's ids in host memory
+    (upload, skycube, download), best of two."""
+    rows, cache = [], {}
+    for kind, m, ref_ms, src in REFERENCE_SWEEPS:
+        if kind not in cache:
+            cache[kind] = datagen.generate(kind, 500000, 16, 1)
+        x = cache[kind]
+        ds = sk.Dataset(ctx, x)
+        dev, info = [], None
+        for rep in range(3):
+            r = sk.skycube(ctx, ds, max_d=m)
+            info = r.info()
+            r.close()
+            if rep:
+                dev.append(ctx.last_device_ms())
+        ds.close()
+        e2e = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            ds = sk.Dataset(ctx, x)
+            r = sk.skycube(ctx, ds, max_d=m)
+            r.download()
+            r.close()
+            ds.close()
+            e2e.append((time.perf_counter() - t0) * 1000.0)
+        rows.append({"workload": f"{kind} 500,000 x 16", "max_d": m,
+                     "device_ms": round(min(dev), 3), "e2e_ms": round(min(e2e), 3),
+                     "total_skyline_ids": info["total_skyline_ids"],
+                     "reference_ms": ref_ms, "reference_source": src})
+    return {"rows": rows,
+            "note": "reference_ms: the authors' SDSC runs on one GPU of their own machine "
+                    "(not a GB300) over their data files; these inputs are seeded synthetic "
+                    "stand-ins with the same shape and distribution family"}
+
+
 def run_ours(args, world, rank, local):
     import torch
     import skycube_gb300 as sk
@@ -398,6 +457,9 @@ def run_ours(args, world, rank, local):
     serving = None
     if rank == 0 and world == 1 and args.serving_queries > 0:
         serving = run_serving(sk, ctx, args)
+    sweeps = None
+    if rank == 0 and world == 1 and not args.no_sweeps:
+        sweeps = run_reference_sweeps(sk, ctx)
 
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
@@ -440,6 +502,8 @@ def run_ours(args, world, rank, local):
         out["plain"] = plain
     if serving:
         out["serving"] = serving
+    if sweeps:
+        out["reference_sweeps"] = sweeps
     if rank == 0:
         print(json.dumps(out), flush=True)
     ctx.close()
