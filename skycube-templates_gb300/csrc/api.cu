@@ -1569,7 +1569,7 @@ int skc_autotune(skc_context* ctx, skc_dataset* ds, const skc_options* base, int
   if (!o.depth) SKC_TRY(try_values(&RunParams::depth, {7, 6, 5, 4, 3}));
   if (!o.pq_size) {
     std::vector<int> pqs;
-    for (int v : {0, 32, 128, 512})
+    for (int v : {0, 32, 128, 512, kMaxPruners})
       if (v == 0 || n > 2ull * (uint64_t)v) pqs.push_back(v);
     SKC_TRY(try_values(&RunParams::pq_size, pqs));
   }
