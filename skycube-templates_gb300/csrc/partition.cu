@@ -241,6 +241,8 @@ __global__ void __launch_bounds__(1024) k_split_plan(const uint32_t* __restrict_
 //
 // LV (level cutoffs, used on unsliced lists): a thread stops scanning a
 // sorted partition at the first q above its own strength level.
+constexpr uint32_t kFullMask = 0xffffffffu;
+
 template <int NA, bool LV>
 __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
   constexpr int NW = (NA + 3) / 4;
@@ -248,7 +250,6 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
   __shared__ uint4 q_cells[TQ];
   __shared__ float q_x[NA][TQ];
   __shared__ uint16_t q_sum[LV ? TQ : 1];
-  __shared__ uint32_t s_conf_end;
 
   __shared__ unsigned long long s_total;
   // CTAs go in partition rank order (lattice level: lower partitions first).
@@ -292,7 +293,6 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
 
   uint8_t st = 0;
   bool done = !valid;
-  bool all_done = false;
   // Sort-filter bound: a q that dominates p, even weakly, has every cell
   // <= p's, so its cell sum and strength level are <= p's. Inside a
   // partition q's ascend in level, so a thread is finished with the
@@ -321,8 +321,14 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
     s_lo = total * sp / splits;
     s_hi = total * (sp + 1) / splits;
   }
-  uint64_t acc = 0;  // q's of the partitions before si (uniform over the CTA)
-  for (uint32_t si = s0; si < s1 && !all_done && acc < s_hi; ++si) {
+  uint64_t acc = 0;  // q's of the partitions before si
+  // Each warp streams the q's through its own 32-entry slice of the tile
+  // arrays and stops on its own: no CTA barrier inside the loop, so a warp
+  // whose points are all settled does not wait for the slowest warp.
+  const int lane = threadIdx.x & 31;
+  const uint32_t wbase = threadIdx.x & ~31u;  // this warp's slice
+  bool wdone = false;  // every point of the warp is settled
+  for (uint32_t si = s0; si < s1 && !wdone && acc < s_hi; ++si) {
     const uint32_t qb = a.sub_list[si];
     uint32_t qbeg = a.boff[qb];
     uint32_t qend = a.boff[qb + 1];
@@ -337,34 +343,34 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
     bool beyond = false;  // past this thread's level in this partition
     bool conf = false;
     if (use_conf && qb != b) {
-      if (threadIdx.x == 0) {
-        uint32_t e = 0xffffffffu;
+      uint32_t e = 0xffffffffu;
+      if (lane == 0) {
         const uint32_t need = a.items[qb + 1] - a.items[qb];
         if (atomicAdd(&a.pdone[qb], 0u) == need) {
           __threadfence();
           e = qbeg + atomicAdd(&a.ccount[qb], 0u);
         }
-        s_conf_end = e;
       }
-      __syncthreads();
-      if (s_conf_end != 0xffffffffu) {
+      e = __shfl_sync(kFullMask, e, 0);
+      if (e != 0xffffffffu) {
+        __threadfence();  // the list's entries are read after its count
         conf = true;
-        qend = s_conf_end;
+        qend = e;
       }
     }
     const uint4* qc = conf ? a.conf_cells : a.cells;
     const float* qxs = conf ? a.conf_x : a.xs;
     bool first = true;
-    for (uint32_t base = qbeg; base < qend; base += TQ) {
+    for (uint32_t base = qbeg; base < qend; base += 32) {
       // Without level cutoffs, or on a partition's first tile (nobody is
-      // beyond yet), the vote is "every point of the CTA is strictly
-      // dominated": the CTA is finished.
-      if (__syncthreads_and(done || (LV && beyond))) {
-        if (!LV || first) all_done = true;
+      // beyond yet), the vote is "every point of the warp is strictly
+      // dominated": the warp is finished.
+      if (__all_sync(kFullMask, done || (LV && beyond))) {
+        if (!LV || first) wdone = true;
         break;
       }
       first = false;
-      const uint32_t j = base + threadIdx.x;
+      const uint32_t j = base + lane;
       if (j < qend) {
         // Confirmed lists are written during this launch by other SMs: read
         // them through L2 (ld.cg), never from a possibly stale L1 line.
@@ -381,16 +387,16 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
         q_cells[threadIdx.x] = qcl;
         if constexpr (LV) q_sum[threadIdx.x] = (uint16_t)cell_sum_na<NA>(qcl);
       }
-      __syncthreads();
+      __syncwarp();
       if (!done && !(LV && beyond)) {
-        uint32_t lim = min((uint32_t)TQ, qend - base);
+        uint32_t lim = min(32u, qend - base);
         if (LV && !conf && sum_cut != 0xffffffffu) {
           // First q of the tile above p's level (levels ascend in a sorted
           // partition; confirmed lists are unordered and fully scanned).
           uint32_t lo = 0, hi = lim;
           while (lo < hi) {
             const uint32_t mid = (lo + hi) >> 1;
-            if (q_sum[mid] >= sum_cut) hi = mid; else lo = mid + 1;
+            if (q_sum[wbase + mid] >= sum_cut) hi = mid; else lo = mid + 1;
           }
           if (lo < lim) {
             lim = lo;
@@ -398,7 +404,7 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
           }
         }
         for (uint32_t t = 0; t < lim; ++t) {
-          const uint4 q = q_cells[t];
+          const uint4 q = q_cells[wbase + t];
           uint32_t worse = 0;  // guard bits where cell(q) > cell(p)
 #pragma unroll
           for (int w = 0; w < NW; ++w) worse |= ~(pH[w] - word_of(q, w)) & hS[w];
@@ -415,7 +421,7 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
           bool le = true, lt_any = false, lt_all = true;
 #pragma unroll
           for (int k = 0; k < NA; ++k) {
-            const float v = q_x[k][t];
+            const float v = q_x[k][wbase + t];
             le &= (v <= pv[k]);
             lt_any |= (v < pv[k]);
             lt_all &= (v < pv[k]);
@@ -430,7 +436,7 @@ __global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
           }
         }
       }
-      __syncthreads();
+      __syncwarp();
     }
   }
   if (valid) {
