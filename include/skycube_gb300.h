@@ -127,6 +127,19 @@ int skc_skycube(skc_context* ctx, skc_dataset* ds, const skc_options* opt,
 
 /* Number of attributes of the result's dataset and number of candidate
  * points (full-space skyline plus extended skyline). */
+/* Which computation produced the result (SKC_FORM_*), and for
+ * SKC_FORM_LEVELS how many cuboids exceeded the level kernels' capacities
+ * and went through the per-cuboid pipeline instead. No reference
+ * counterpart (the suite's algorithm is chosen by -s). */
+enum {
+  SKC_FORM_BITMAPS = 1, /* per-point dominated-subspace bitmaps, one launch */
+  SKC_FORM_CUBOIDS = 2, /* per cuboid, one launch sequence each (plain SDSC) */
+  SKC_FORM_LEVELS = 3,  /* per cuboid, one lattice level per launch pair:
+                           batched capped skycubes, max_d <= 4 and <= d - 2 */
+  SKC_FORM_SKYLINE = 4  /* a single-subspace skyline query */
+};
+int skc_result_form(skc_result* res, int* form, int* fallbacks);
+
 int skc_result_info(skc_result* res, int* d, uint64_t* n_candidates,
                     uint64_t* total_skyline_ids);
 

@@ -541,22 +541,19 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
 }
 
 // The suite's per-cuboid schedule (PLAIN/SDSC).
-static int run_sdsc_plain(Exec& E, skc_dataset* ds, int max_d,
-                          int depth_of_call, Arena& A, FullSpace& F,
-                          skc_result* R, Tracer& T) {
-  skc_context* ctx = E.ctx;
-  cudaStream_t s = E.stream;
-  const int d = ds->d;
-  const uint32_t nsub = 1u << d, full = nsub - 1;
-  std::vector<uint32_t*> sky(nsub, nullptr), ext(nsub, nullptr);
-  std::vector<uint64_t> nsky(nsub, 0), next(nsub, 0);
-  sky[full] = F.sky;
-  ext[full] = F.ext;
-  nsky[full] = F.h_counts[0];
-  next[full] = F.h_counts[1];
-
-  uint64_t mmax = nsky[full] + next[full];
+// Scratch of the single-cuboid pipeline for lists of up to mmax entries.
+struct CuboidScratch {
   PartScratch ps;
+  uint32_t *cand = nullptr, *d_m = nullptr, *blk0 = nullptr, *blk1 = nullptr, *cnt = nullptr;
+  uint8_t* status = nullptr;
+  uint32_t* h_cnt = nullptr;  // pinned [2]
+  ~CuboidScratch() {
+    if (h_cnt) cudaFreeHost(h_cnt);
+  }
+};
+
+static int cuboid_scratch(Arena& A, int d, uint64_t mmax, CuboidScratch* cs) {
+  PartScratch& ps = cs->ps;
   const uint32_t Kmax = 1u << kMaxPartitionDims;
   SKC_TRY(A.alloc(&ps.keys, mmax));
   SKC_TRY(A.alloc(&ps.sorted, mmax));
@@ -572,68 +569,51 @@ static int run_sdsc_plain(Exec& E, skc_dataset* ds, int max_d,
   SKC_TRY(A.alloc(&ps.cursor, kMaxSortBuckets + 1));
   SKC_TRY(A.alloc(&ps.fine, kMaxSortBuckets + 1));
   SKC_TRY(A.alloc(&ps.items, Kmax + 1));
-  uint32_t *cand, *d_m, *blk0, *blk1, *cnt;
-  uint8_t* status;
-  SKC_TRY(A.alloc(&cand, mmax));
-  SKC_TRY(A.alloc(&status, round_up(mmax, 4)));
-  SKC_TRY(A.alloc(&d_m, 1));
+  SKC_TRY(A.alloc(&cs->cand, mmax));
+  SKC_TRY(A.alloc(&cs->status, round_up(mmax, 4)));
+  SKC_TRY(A.alloc(&cs->d_m, 1));
   const uint64_t nblk = (mmax + 1023) / 1024 + 1;
-  SKC_TRY(A.alloc(&blk0, nblk));
-  SKC_TRY(A.alloc(&blk1, nblk));
-  SKC_TRY(A.alloc(&cnt, 2));
-  uint32_t* h_cnt = nullptr;
-  SKC_CUDA(cudaMallocHost(&h_cnt, 2 * sizeof(uint32_t)));
+  SKC_TRY(A.alloc(&cs->blk0, nblk));
+  SKC_TRY(A.alloc(&cs->blk1, nblk));
+  SKC_TRY(A.alloc(&cs->cnt, 2));
+  SKC_CUDA(cudaMallocHost(&cs->h_cnt, 2 * sizeof(uint32_t)));
+  return SKC_OK;
+}
 
-  int st = SKC_OK;
-  for (int lev = d - 1; lev >= 1 && st == SKC_OK; --lev) {
-    if (lev > max_d) continue;
-    for (uint32_t c = 1; c < full && st == SKC_OK; ++c) {
-      if (__builtin_popcount(c) != lev) continue;
-      // Parents in the order generate_lattice lists them (descending index).
-      uint32_t par[kMaxDims];
-      int np = 0;
-      for (int j = d - 1; j >= 0; --j)
-        if (!(c & (1u << j))) par[np++] = c | (1u << j);
-      uint32_t src = full;
-      if (nsky[par[0]] != 0) {
-        src = par[0];
-        uint64_t best = nsky[src] + next[src];
-        for (int i = 1; i < np; ++i) {
-          const uint64_t v = nsky[par[i]] + next[par[i]];
-          if (v < best) { best = v; src = par[i]; }
-        }
-      }
-      const uint64_t mc = nsky[src] + next[src];
-      if (mc == 0) continue;
-      auto fail = [&](int code) { st = code; };
-      // Candidates = parent skyline + extended skyline, merged ascending so
-      // every output list stays ascending (compaction keeps list order).
-      if ((st = launch_merge_disjoint(s, sky[src], (uint32_t)nsky[src], ext[src], (uint32_t)next[src], cand)) != SKC_OK) break;
-      cudaError_t e = cudaSuccess;
-      if ((st = launch_set_u32(s, d_m, (uint32_t)mc)) != SKC_OK) break;
-      LevelTables LT;
-      if ((st = level_tables(ctx, partition_dims(c), &LT)) != SKC_OK) break;
-      PartitionSkylineArgs pa{cand, F.cells, ds->x, ds->n_pad, d_m, mc, c, status};
-      if ((st = launch_partition_skyline(s, d, depth_of_call, LT, pa, ps)) != SKC_OK) break;
-      uint32_t *osky, *oext;
-      if ((st = A.alloc(&osky, mc)) != SKC_OK) break;
-      if ((st = A.alloc(&oext, mc)) != SKC_OK) break;
-      if ((st = launch_status_compact(s, status, cand, d_m, mc, 0, blk0, blk1, osky, oext, cnt, cnt + 1)) != SKC_OK) break;
-      e = cudaMemcpyAsync(h_cnt, cnt, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-      if (e != cudaSuccess) { fail(set_error(SKC_ERR_CUDA, "cuboid %u: %s", c, cudaGetErrorString(e))); break; }
-      sky[c] = osky;
-      ext[c] = oext;
-      nsky[c] = h_cnt[0];
-      next[c] = h_cnt[1];
-    }
-  }
-  cudaFreeHost(h_cnt);
-  SKC_TRY(st);
-  T.mark("per-cuboid skylines");
+// Skyline and extended skyline of cuboid c over an ascending candidate list
+// (both outputs ascending), with the median-partition pipeline; one host
+// round trip for the counts.
+static int cuboid_lists(Exec& E, skc_dataset* ds, FullSpace& F, int depth, Arena& A,
+                        CuboidScratch& cs, uint32_t c, const uint32_t* cand, uint64_t mc,
+                        uint32_t** osky, uint32_t** oext, uint64_t* nsky, uint64_t* next) {
+  cudaStream_t s = E.stream;
+  SKC_TRY(launch_set_u32(s, cs.d_m, (uint32_t)mc));
+  LevelTables LT;
+  SKC_TRY(level_tables(E.ctx, partition_dims(c), &LT));
+  PartitionSkylineArgs pa{cand, F.cells, ds->x, ds->n_pad, cs.d_m, mc, c, cs.status};
+  SKC_TRY(launch_partition_skyline(s, ds->d, depth, LT, pa, cs.ps));
+  SKC_TRY(A.alloc(osky, mc));
+  SKC_TRY(A.alloc(oext, mc));
+  SKC_TRY(launch_status_compact(s, cs.status, cand, cs.d_m, mc, 0, cs.blk0, cs.blk1, *osky,
+                                *oext, cs.cnt, cs.cnt + 1));
+  cudaError_t e = cudaMemcpyAsync(cs.h_cnt, cs.cnt, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return set_error(SKC_ERR_CUDA, "cuboid %u: %s", c, cudaGetErrorString(e));
+  *nsky = cs.h_cnt[0];
+  *next = cs.h_cnt[1];
+  return SKC_OK;
+}
 
-  // Assemble cuboid-indexed CSRs of skylines and extended skylines.
-  for (int pass = 0; pass < 2; ++pass) {
+// Cuboid-indexed CSRs of skylines (and extended skylines when want_ext) from
+// per-cuboid device lists; cuboids above max_d (except the full space) are
+// left empty.
+static int assemble_csr(Exec& E, Arena& A, int d, int max_d, bool want_ext,
+                        const std::vector<uint32_t*>& sky, const std::vector<uint64_t>& nsky,
+                        const std::vector<uint32_t*>& ext, const std::vector<uint64_t>& next,
+                        skc_result* R) {
+  cudaStream_t s = E.stream;
+  const uint32_t nsub = 1u << d, full = nsub - 1;
+  for (int pass = 0; pass < (want_ext ? 2 : 1); ++pass) {
     std::vector<uint64_t> off(nsub + 1, 0);
     const auto& cntv = pass == 0 ? nsky : next;
     const auto& srcv = pass == 0 ? sky : ext;
@@ -667,6 +647,184 @@ static int run_sdsc_plain(Exec& E, skc_dataset* ds, int max_d,
     }
   }
   return SKC_OK;
+}
+
+// Smallest computed parent of c (the full space when none of its parents
+// was computed), as the suite's findMinParent picks it.
+static uint32_t min_parent(uint32_t c, int d, const std::vector<uint64_t>& nsky,
+                           const std::vector<uint64_t>& next, const std::vector<char>& done) {
+  const uint32_t full = (1u << d) - 1;
+  uint32_t src = full;
+  uint64_t best = ~0ull;
+  for (int j = d - 1; j >= 0; --j) {  // parents in generate_lattice's order
+    if (c & (1u << j)) continue;
+    const uint32_t p = c | (1u << j);
+    if (p == full || !done[p]) continue;
+    const uint64_t v = nsky[p] + next[p];
+    if (v < best) {
+      best = v;
+      src = p;
+    }
+  }
+  return src;
+}
+
+static int run_sdsc_plain(Exec& E, skc_dataset* ds, int max_d,
+                          int depth_of_call, Arena& A, FullSpace& F,
+                          skc_result* R, Tracer& T) {
+  const int d = ds->d;
+  const uint32_t nsub = 1u << d, full = nsub - 1;
+  std::vector<uint32_t*> sky(nsub, nullptr), ext(nsub, nullptr);
+  std::vector<uint64_t> nsky(nsub, 0), next(nsub, 0);
+  std::vector<char> done(nsub, 0);
+  sky[full] = F.sky;
+  ext[full] = F.ext;
+  nsky[full] = F.h_counts[0];
+  next[full] = F.h_counts[1];
+  done[full] = 1;
+
+  CuboidScratch cs;
+  SKC_TRY(cuboid_scratch(A, d, nsky[full] + next[full], &cs));
+  for (int lev = d - 1; lev >= 1; --lev) {
+    if (lev > max_d) continue;
+    for (uint32_t c = 1; c < full; ++c) {
+      if (__builtin_popcount(c) != lev) continue;
+      const uint32_t src = min_parent(c, d, nsky, next, done);
+      const uint64_t mc = nsky[src] + next[src];
+      done[c] = 1;
+      if (mc == 0) continue;
+      // Candidates = parent skyline + extended skyline, merged ascending so
+      // every output list stays ascending (compaction keeps list order).
+      SKC_TRY(launch_merge_disjoint(E.stream, sky[src], (uint32_t)nsky[src], ext[src],
+                                    (uint32_t)next[src], cs.cand));
+      SKC_TRY(cuboid_lists(E, ds, F, depth_of_call, A, cs, c, cs.cand, mc, &sky[c], &ext[c],
+                           &nsky[c], &next[c]));
+    }
+  }
+  T.mark("per-cuboid skylines");
+  return assemble_csr(E, A, d, max_d, true, sky, nsky, ext, next, R);
+}
+
+// Capped skycubes (max_d <= kLvMaxDims) by lattice level (levels.cu): every
+// cuboid of a level in one filter launch and one sort-filter launch per
+// group of cuboids, each from its smallest computed parent's skyline +
+// extended skyline or the full space's candidates. Cuboids over the
+// kernel's capacities go through the single-cuboid pipeline.
+constexpr uint64_t kLvScratchBytes = 2048ull << 20;  // survivor scratch per group
+constexpr uint32_t kLvMaxSurvivors = 262144;         // per cuboid
+
+static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d, int depth,
+                      Arena& A, FullSpace& F, skc_result* R, Tracer& T) {
+  cudaStream_t s = E.stream;
+  const int d = ds->d;
+  const uint32_t nsub = 1u << d, full = nsub - 1;
+  std::vector<uint32_t*> sky(nsub, nullptr), ext(nsub, nullptr);
+  std::vector<uint64_t> nsky(nsub, 0), next(nsub, 0);
+  std::vector<const uint32_t*> lst(nsub, nullptr);  // sky + ext of a computed cuboid
+  std::vector<char> done(nsub, 0);
+  sky[full] = F.sky;
+  ext[full] = F.ext;
+  nsky[full] = F.h_counts[0];
+  next[full] = F.h_counts[1];
+  lst[full] = F.cand;
+  done[full] = 1;
+  CuboidScratch cs;
+  bool cs_ready = false;
+  int fallbacks = 0;
+
+  for (int lev = max_d; lev >= 1; --lev) {
+    std::vector<uint32_t> cubs;
+    for (uint32_t c = 1; c < full; ++c)
+      if (__builtin_popcount(c) == lev) cubs.push_back(c);
+    const uint32_t nc = (uint32_t)cubs.size();
+    std::vector<uint32_t> src(nc), hn(nc);
+    std::vector<const uint32_t*> hl(nc);
+    uint64_t maxn = 0;
+    for (uint32_t i = 0; i < nc; ++i) {
+      src[i] = min_parent(cubs[i], d, nsky, next, done);
+      hl[i] = lst[src[i]];
+      hn[i] = (uint32_t)(nsky[src[i]] + next[src[i]]);
+      maxn = std::max<uint64_t>(maxn, hn[i]);
+    }
+    const uint32_t cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(maxn, kLvMaxSurvivors));
+    const uint32_t G = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>(nc, kLvScratchBytes / ((uint64_t)cap * 10)));
+    uint32_t *d_masks, *d_n, *slot, *outs, *cnt, *surv_id, *srt;
+    const uint32_t** d_lists;
+    uint16_t* surv_key;
+    SKC_TRY(A.alloc(&d_masks, nc));
+    SKC_TRY(A.alloc(&d_n, nc));
+    SKC_TRY(A.alloc(&d_lists, nc));
+    SKC_TRY(A.alloc(&slot, (uint64_t)nc * kLvSlot));
+    SKC_TRY(A.alloc(&outs, 3ull * nc));
+    SKC_TRY(A.alloc(&cnt, G));
+    SKC_TRY(A.alloc(&surv_id, (uint64_t)G * cap));
+    SKC_TRY(A.alloc(&surv_key, (uint64_t)G * cap));
+    SKC_TRY(A.alloc(&srt, (uint64_t)G * cap));
+    SKC_CUDA(cudaMemcpyAsync(d_masks, cubs.data(), nc * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    SKC_CUDA(cudaMemcpyAsync(d_n, hn.data(), nc * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    SKC_CUDA(cudaMemcpyAsync(d_lists, hl.data(), nc * sizeof(void*), cudaMemcpyHostToDevice, s));
+    for (uint32_t g0 = 0; g0 < nc; g0 += G) {
+      const uint32_t ng = std::min(G, nc - g0);
+      SKC_CUDA(cudaMemsetAsync(cnt, 0, ng * sizeof(uint32_t), s));
+      LvArgs a{ng, d_masks + g0, d_lists + g0, d_n + g0, (uint32_t)maxn, F.cells, ds->x,
+               ds->n_pad, cap, cnt, surv_id, surv_key, srt, slot + (uint64_t)g0 * kLvSlot,
+               outs + g0, outs + nc + g0, outs + 2ull * nc + g0};
+      SKC_TRY(launch_lv_filter(s, a));
+      SKC_TRY(launch_lv_sfs(s, a));
+    }
+    std::vector<uint32_t> h(3ull * nc);
+    SKC_CUDA(cudaMemcpyAsync(h.data(), outs, 3ull * nc * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    SKC_CUDA(cudaStreamSynchronize(s));  // also keeps the uploaded host vectors alive
+    for (uint32_t i = 0; i < nc; ++i) {
+      const uint32_t c = cubs[i];
+      if (h[2ull * nc + i] == 0) {
+        sky[c] = slot + (uint64_t)i * kLvSlot;
+        nsky[c] = h[i];
+        ext[c] = sky[c] + nsky[c];
+        next[c] = h[nc + i];
+        lst[c] = sky[c];
+        done[c] = 1;
+        continue;
+      }
+      // Over a capacity: the single-cuboid pipeline on an ascending list.
+      if (!cs_ready) {
+        SKC_TRY(cuboid_scratch(A, d, F.h_counts[2], &cs));
+        cs_ready = true;
+      }
+      ++fallbacks;
+      const uint32_t p = src[i];
+      const uint64_t mc = nsky[p] + next[p];
+      const uint32_t* cand = F.cand;
+      if (p != full) {
+        SKC_TRY(launch_merge_disjoint(s, sky[p], (uint32_t)nsky[p], ext[p], (uint32_t)next[p], cs.cand));
+        cand = cs.cand;
+      }
+      SKC_TRY(cuboid_lists(E, ds, F, depth, A, cs, c, cand, mc, &sky[c], &ext[c], &nsky[c], &next[c]));
+      uint32_t* merged;
+      SKC_TRY(A.alloc(&merged, std::max<uint64_t>(1, nsky[c] + next[c])));
+      SKC_TRY(launch_merge_disjoint(s, sky[c], (uint32_t)nsky[c], ext[c], (uint32_t)next[c], merged));
+      lst[c] = merged;
+      done[c] = 1;
+    }
+    static const char* const kLevelMark[] = {"", "level 1", "level 2", "level 3", "level 4"};
+    T.mark(kLevelMark[lev]);
+  }
+  R->level_fallbacks = fallbacks;
+  const bool want_ext = o.want_extended || o.algo == SKC_ALGO_SDSC;
+  return assemble_csr(E, A, d, max_d, want_ext, sky, nsky, ext, next, R);
+}
+
+// The level form replaces the bitmaps for batched capped skycubes of small
+// caps on enough candidates (below that the bitmap kernel is as fast), when
+// no per-point bitmaps are wanted and no plan is being recorded (the level
+// form syncs per level).
+constexpr uint64_t kLvMinCandidates = 4096;
+static bool use_levels(const Exec& E, const skc_dataset* ds, const skc_options& o, int max_d,
+                       const FullSpace& F) {
+  return !E.plan && o.mode == SKC_MODE_BATCHED && !o.want_bitmaps && max_d <= kLvMaxDims &&
+         max_d <= ds->d - 2 && F.h_counts[2] >= kLvMinCandidates && ds->n < (1ull << 31) &&
+         F.h_counts[2] <= 65535ull * kLvChunk;  // filter grid's y extent
 }
 
 static int auto_depth(uint64_t n, int d) {
@@ -1204,10 +1362,16 @@ static int skycube_exec(Exec& E, skc_dataset* ds, const skc_options* opt, skc_re
     if (st == SKC_OK) {
       R->n_cand = F.h_counts[2];
       if (o.subspace) {
+        R->form = SKC_FORM_SKYLINE;
         st = run_single_cuboid(E, ds, o.subspace, P, A, F, R, T);
       } else if (o.algo == SKC_ALGO_SDSC && o.mode == SKC_MODE_PLAIN) {
+        R->form = SKC_FORM_CUBOIDS;
         st = run_sdsc_plain(E, ds, max_d, depth, A, F, R, T);
+      } else if (use_levels(E, ds, o, max_d, F)) {
+        R->form = SKC_FORM_LEVELS;
+        st = run_levels(E, ds, o, max_d, depth, A, F, R, T);
       } else {
+        R->form = SKC_FORM_BITMAPS;
         st = run_bitmaps(E, ds, o, P, max_d, A, F, R, T);
       }
     }
@@ -1420,6 +1584,7 @@ int skc_plan_execute(skc_plan* p, skc_result** out) {
   R->stream = s;
   R->d = p->outs.d;
   R->max_d = p->outs.max_d;
+  R->form = SKC_FORM_BITMAPS;
   R->algo = p->outs.algo;
   R->n_cand = m;
   R->total_ids = p->h_stats[1];
@@ -1626,6 +1791,14 @@ int skc_tuning_clear(skc_context* ctx) {
   if (!ctx) return set_error(SKC_ERR_INVALID, "NULL context");
   std::lock_guard<std::mutex> lock(ctx->mu);
   ctx->tunings.clear();
+  return SKC_OK;
+}
+
+int skc_result_form(skc_result* r, int* form, int* fallbacks) {
+  clear_error();
+  if (!r) return set_error(SKC_ERR_INVALID, "NULL result");
+  if (form) *form = r->form;
+  if (fallbacks) *fallbacks = r->level_fallbacks;
   return SKC_OK;
 }
 
@@ -1843,6 +2016,13 @@ static uint64_t footprint_estimate(uint64_t n, int d, const skc_options& o, bool
     b += 2 * (uint64_t)d * np * 4 + n * (16 * 3 + 4 * 3);
     b += n * W * 4 * (ext ? 3 : 2);  // bitmaps + compaction
     b += n * 4 * std::min<uint64_t>(1ull << d, 64);  // id lists
+    const int md = (o.max_d <= 0 || o.max_d > d) ? d : o.max_d;
+    if (md <= kLvMaxDims && md <= d - 2) {  // the level form may run instead
+      uint64_t cub = 1;  // cuboids of the widest level, C(d, md)
+      for (int k = 0; k < md; ++k) cub = cub * (uint64_t)(d - k) / (uint64_t)(k + 1);
+      b += std::min<uint64_t>(kLvScratchBytes, cub * std::min<uint64_t>(n, kLvMaxSurvivors) * 10);
+      b += (uint64_t)md * cub * kLvSlot * 4 + n * (16 * 2 + 4 * 6) + 2 * (uint64_t)d * np * 4;
+    }
   }
   return b;
 }

@@ -136,6 +136,8 @@ struct skc_result {
   int algo = 0;
   uint64_t n_cand = 0;
   uint64_t total_ids = 0;
+  int form = 0;             // SKC_FORM_*
+  int level_fallbacks = 0;  // SKC_FORM_LEVELS: cuboids over the kernel's capacities
   // Device CSR of skylines and (optionally) extended skylines, indexed by
   // cuboid mask: ids of c are ids[off[c] .. off[c+1]).
   uint64_t* d_off = nullptr;

@@ -218,6 +218,40 @@ uint32_t compact_tiles(uint64_t m_max);
 int launch_bits_count(cudaStream_t s, const CompactArgs& a);
 int launch_bits_write(cudaStream_t s, const CompactArgs& a);
 
+// levels.cu: capped skycubes by lattice level (cuboids of at most
+// kLvMaxDims attributes), one CTA per cuboid for the sort-filter skyline.
+constexpr int kLvMaxDims = 4;
+constexpr uint32_t kLvPruners = 32;    // per cuboid, from a strided sample
+constexpr uint32_t kLvSample = 1024;   // sampled list entries
+constexpr uint32_t kLvChunk = 4096;    // list entries per filter CTA
+constexpr uint32_t kLvThreads = 1024;  // sort-filter CTA, one batch per pass
+constexpr uint32_t kLvWin = 2048;      // skyline points per cuboid
+constexpr uint32_t kLvExt = 4096;      // extended-skyline points per cuboid
+constexpr uint32_t kLvSlot = kLvWin + kLvExt;  // output ids per cuboid
+constexpr uint32_t kLvSortCap = 8192;  // power of two >= kLvSlot
+constexpr uint32_t kLvKeyBins = 127 * kLvMaxDims + 1;  // cell sums
+struct LvArgs {
+  uint32_t ncub;                 // cuboids of this launch
+  const uint32_t* masks;         // [ncub]
+  const uint32_t* const* lists;  // [ncub] candidate ids
+  const uint32_t* list_n;        // [ncub]
+  uint32_t max_list;             // upper bound of list_n
+  const uint4* cells;            // point id -> grid cells
+  const float* x;                // attribute-major points, pitch n_pad
+  uint64_t n_pad;
+  uint32_t cap;                  // survivors kept per cuboid
+  uint32_t* cnt;                 // [ncub] survivors (zeroed before the filter)
+  uint32_t* surv_id;             // [ncub * cap]
+  uint16_t* surv_key;            // [ncub * cap]
+  uint32_t* srt;                 // [ncub * cap] survivors by cell sum
+  uint32_t* slot;                // [ncub * kLvSlot]: skyline ids, then extended
+  uint32_t* o_nsky;              // [ncub]
+  uint32_t* o_next;              // [ncub]
+  uint32_t* o_flag;              // [ncub] 1: over a capacity, not computed
+};
+int launch_lv_filter(cudaStream_t s, const LvArgs& a);
+int launch_lv_sfs(cudaStream_t s, const LvArgs& a);
+
 void upload_submask_table();
 
 }  // namespace skc

@@ -1,0 +1,492 @@
+// Capped skycubes by lattice level: the skyline and extended skyline of
+// every cuboid of one level, all cuboids of the level in one launch pair.
+// This is the per-cuboid computation of the suite's SDSC (each cuboid from
+// its smallest computed parent's skyline + extended skyline, or from the
+// full space's when the parents lie above the cap: findMinParent and
+// gpu_processing_thread, src/sdsc/SDSC.cu:76-137,366-376), batched over a
+// level instead of one SkyAlign call per cuboid, for cuboids of at most
+// kLvMaxDims attributes.
+//
+// Per cuboid S and candidate list L:
+//  1. k_lv_filter: 32 pruners = the lowest cell sums over S of a 1,024-entry
+//     strided sample of L; every entry of L that a pruner strictly dominates
+//     on S is dropped (exact float test on equal cells). If a dropped q
+//     dominated a kept p, the pruner that drops q would strictly dominate p,
+//     so the kept entries (survivors) decide each other's status alone.
+//  2. k_lv_sfs: the survivors, counting-sorted by cell sum over S (a
+//     dominator's sum is never larger), go through a sort-filter skyline in
+//     batches of 1,024: each entry is tested against the window of skyline
+//     points found so far (strict domination drops it), the batch's
+//     remaining entries against each other, and the batch's new skyline
+//     points join the window. An entry can only be dominated by an entry of
+//     equal cell sum that comes later if all their cells on S are equal; a
+//     last pass tests each skyline and extended entry against the survivors
+//     of its cell-sum bucket with equal cells. Output: [skyline | extended
+//     skyline] ids, each ascending, in the cuboid's slot.
+// A cuboid whose survivors, skyline or extended skyline exceed the
+// shared-memory capacities is flagged; the host then computes it with the
+// single-cuboid pipeline.
+#include "kernels.cuh"
+
+namespace skc {
+
+namespace {
+
+constexpr uint32_t kWarpAll = 0xffffffffu;
+
+struct CubAttrs {
+  int na;
+  int att[kLvMaxDims];
+  uint32_t gm;  // guard bits of bytes 0 .. na-1
+};
+
+__device__ __forceinline__ CubAttrs cub_attrs(uint32_t S) {
+  CubAttrs A;
+  A.na = min(__popc(S), kLvMaxDims);
+#pragma unroll
+  for (int a = 0; a < kLvMaxDims; ++a)  // index of the (a+1)-th set bit of S
+    A.att[a] = a < A.na ? (int)__fns(S, 0, a + 1) : 0;
+  A.gm = 0;
+#pragma unroll
+  for (int a = 0; a < kLvMaxDims; ++a)
+    if (a < A.na) A.gm |= 0x80u << (8 * a);
+  return A;
+}
+
+// Byte a = the cell of attribute att[a] (cells are < 128).
+__device__ __forceinline__ uint32_t lv_pack(const uint4& c, const CubAttrs& A) {
+  uint32_t r = 0;
+#pragma unroll
+  for (int a = 0; a < kLvMaxDims; ++a)
+    if (a < A.na) {
+      const int k = A.att[a];
+      r |= ((word_of(c, k >> 2) >> (8 * (k & 3))) & 0x7fu) << (8 * a);
+    }
+  return r;
+}
+
+__device__ __forceinline__ uint32_t lv_key(uint32_t pc) {
+  return (pc & 0xffu) + ((pc >> 8) & 0xffu) + ((pc >> 16) & 0xffu) + (pc >> 24);
+}
+
+__device__ __forceinline__ void lv_load(const float* __restrict__ x, uint64_t n_pad, uint32_t id,
+                                        const CubAttrs& A, float* v) {
+#pragma unroll
+  for (int a = 0; a < kLvMaxDims; ++a)
+    v[a] = a < A.na ? x[(uint64_t)A.att[a] * n_pad + id] : 0.f;
+}
+
+// 0: q does not dominate p on S; 1: dominates; 2: strictly dominates.
+__device__ __forceinline__ int lv_dom(uint32_t qc, const float* qv, uint32_t pc, const float* pv,
+                                      const CubAttrs& A) {
+  if ((ge_bytes(pc | kGuard, qc) & A.gm) != A.gm) return 0;  // a cell of q above p's
+  const uint32_t eq = ge_bytes(qc | kGuard, pc) & A.gm;       // equal cells
+  if (!eq) return 2;
+  bool any_lt = eq != A.gm, all_lt = true;
+#pragma unroll
+  for (int a = 0; a < kLvMaxDims; ++a) {
+    if (eq & (0x80u << (8 * a))) {
+      if (qv[a] > pv[a]) return 0;
+      if (qv[a] < pv[a]) any_lt = true;
+      else all_lt = false;
+    }
+  }
+  if (!any_lt) return 0;
+  return all_lt ? 2 : 1;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_lv_filter(
+    const uint32_t* __restrict__ masks, const uint32_t* const* __restrict__ lists,
+    const uint32_t* __restrict__ list_n, const uint4* __restrict__ cells,
+    const float* __restrict__ x, uint64_t n_pad, uint32_t cap, uint32_t* __restrict__ cnt,
+    uint32_t* __restrict__ surv_id, uint16_t* __restrict__ surv_key) {
+  __shared__ uint32_t hist[kLvKeyBins];
+  __shared__ uint32_t s_thr, s_np, s_n, s_base;
+  __shared__ uint32_t pr_c[kLvPruners];
+  __shared__ float pr_v[kLvMaxDims][kLvPruners];
+  // The chunk's survivors are staged here and appended with one atomic.
+  __shared__ uint32_t st_id[kLvChunk];
+  __shared__ uint16_t st_key[kLvChunk];
+  // Consecutive CTAs take different cuboids, spreading the appends.
+  const uint32_t c = blockIdx.x;
+  const uint32_t n = list_n[c];
+  const uint32_t beg = blockIdx.y * kLvChunk;
+  if (beg >= n) return;  // uniform over the CTA
+  const uint32_t end = min(n, beg + kLvChunk);
+  const uint32_t* __restrict__ L = lists[c];
+  const CubAttrs A = cub_attrs(masks[c]);
+  const int tid = threadIdx.x, lane = tid & 31;
+
+  // Pruners: the lowest cell sums of a strided sample (every CTA of the
+  // cuboid picks the same ones).
+  const uint32_t ns = min(n, kLvSample);
+  for (uint32_t i = tid; i < kLvKeyBins; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  constexpr int kPer = kLvSample / 256;
+  uint32_t sid[kPer], skey[kPer];
+#pragma unroll
+  for (int r = 0; r < kPer; ++r) {
+    const uint32_t i = tid + 256u * r;
+    sid[r] = 0;
+    skey[r] = 0xffffffffu;
+    if (i < ns) {
+      sid[r] = L[(uint64_t)i * n / ns];
+      skey[r] = lv_key(lv_pack(cells[sid[r]], A));
+      atomicAdd(&hist[skey[r]], 1u);
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t acc = 0, t = kLvKeyBins - 1;
+    for (uint32_t k = 0; k < kLvKeyBins; ++k) {
+      if (acc + hist[k] >= kLvPruners) {
+        t = k;
+        break;
+      }
+      acc += hist[k];
+    }
+    s_thr = t;
+    s_np = 0;
+    s_n = 0;
+  }
+  __syncthreads();
+  const uint32_t thr = s_thr;
+  for (int pass = 0; pass < 2; ++pass) {  // sums below the threshold, then at it
+#pragma unroll
+    for (int r = 0; r < kPer; ++r) {
+      const bool take = pass == 0 ? skey[r] < thr : skey[r] == thr;
+      if (take) {
+        const uint32_t k = atomicAdd(&s_np, 1u);
+        if (k < kLvPruners) {
+          pr_c[k] = lv_pack(cells[sid[r]], A);
+          float v[kLvMaxDims];
+          lv_load(x, n_pad, sid[r], A, v);
+#pragma unroll
+          for (int a = 0; a < kLvMaxDims; ++a) pr_v[a][k] = v[a];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  const uint32_t np = min(s_np, kLvPruners);
+
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  for (uint32_t base = beg; base < end; base += blockDim.x) {
+    const uint32_t i = base + tid;
+    const bool valid = i < end;
+    uint32_t id = 0, pc = 0;
+    bool dead = false;
+    if (valid) {
+      id = L[i];
+      pc = lv_pack(cells[id], A);
+      float pv[kLvMaxDims];
+      bool have_v = false;
+      for (uint32_t j = 0; j < np; ++j) {
+        const uint32_t qc = pr_c[j];
+        if ((ge_bytes(pc | kGuard, qc) & A.gm) != A.gm) continue;
+        const uint32_t eq = ge_bytes(qc | kGuard, pc) & A.gm;
+        if (!eq) {
+          dead = true;
+          break;
+        }
+        if (!have_v) {
+          lv_load(x, n_pad, id, A, pv);
+          have_v = true;
+        }
+        bool strict = true;
+#pragma unroll
+        for (int a = 0; a < kLvMaxDims; ++a)
+          if ((eq & (0x80u << (8 * a))) && !(pr_v[a][j] < pv[a])) strict = false;
+        if (strict) {
+          dead = true;
+          break;
+        }
+      }
+    }
+    const bool keep = valid && !dead;
+    const uint32_t live = __ballot_sync(kWarpAll, keep);
+    uint32_t pos0 = 0;
+    if (lane == 0 && live) pos0 = atomicAdd(&s_n, (uint32_t)__popc(live));
+    pos0 = __shfl_sync(kWarpAll, pos0, 0);
+    if (keep) {
+      const uint32_t pos = pos0 + __popc(live & lt_mask);  // < kLvChunk
+      st_id[pos] = id;
+      st_key[pos] = (uint16_t)lv_key(pc);
+    }
+  }
+  __syncthreads();
+  const uint32_t ns_kept = s_n;
+  if (tid == 0) s_base = ns_kept ? atomicAdd(&cnt[c], ns_kept) : 0u;
+  __syncthreads();
+  const uint32_t b0 = s_base;
+  for (uint32_t k = tid; k < ns_kept; k += blockDim.x) {
+    const uint32_t pos = b0 + k;
+    if (pos < cap) {
+      surv_id[(uint64_t)c * cap + pos] = st_id[k];
+      surv_key[(uint64_t)c * cap + pos] = st_key[k];
+    }
+  }
+}
+
+// Shared memory of k_lv_sfs, in bytes.
+static constexpr size_t kLvSfsSmem =
+    (2 * (kLvKeyBins + 1)) * 4 +                                   // bucket offsets, cursors
+    kLvWin * (4 + 4 * kLvMaxDims + 4 + 1) +                        // window
+    kLvExt * (4 + 1) +                                             // extended entries
+    kLvThreads * (4 + 4 * kLvMaxDims + 4 + 2 + 1) +                // batch
+    kLvSortCap * 4 + 64;                                           // sort buffer, counters
+
+__global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
+    const uint32_t* __restrict__ masks, const uint4* __restrict__ cells,
+    const float* __restrict__ x, uint64_t n_pad, uint32_t cap, const uint32_t* __restrict__ cnt,
+    const uint32_t* __restrict__ surv_id, const uint16_t* __restrict__ surv_key,
+    uint32_t* __restrict__ srt, uint32_t* __restrict__ slot, uint32_t* __restrict__ o_nsky,
+    uint32_t* __restrict__ o_next, uint32_t* __restrict__ o_flag) {
+  extern __shared__ __align__(16) unsigned char lv_smem[];
+  const uint32_t c = blockIdx.x;
+  const int tid = threadIdx.x;
+  const uint32_t n = cnt[c];
+  if (n > cap) {  // survivors beyond the scratch: the host takes this cuboid
+    if (tid == 0) {
+      o_flag[c] = 1;
+      o_nsky[c] = 0;
+      o_next[c] = 0;
+    }
+    return;
+  }
+  const CubAttrs A = cub_attrs(masks[c]);
+  const uint64_t off = (uint64_t)c * cap;
+
+  uint32_t* kb = reinterpret_cast<uint32_t*>(lv_smem);   // [kLvKeyBins + 1]
+  uint32_t* cur = kb + kLvKeyBins + 1;                    // [kLvKeyBins + 1]
+  uint32_t* w_c = cur + kLvKeyBins + 1;                   // [kLvWin]
+  float* w_v = reinterpret_cast<float*>(w_c + kLvWin);    // [kLvMaxDims][kLvWin]
+  uint32_t* w_pos = reinterpret_cast<uint32_t*>(w_v + kLvMaxDims * kLvWin);
+  uint32_t* e_pos = w_pos + kLvWin;                       // [kLvExt]
+  uint32_t* b_c = e_pos + kLvExt;                         // [kLvThreads]
+  float* b_v = reinterpret_cast<float*>(b_c + kLvThreads);  // [kLvMaxDims][kLvThreads]
+  uint32_t* b_pos = reinterpret_cast<uint32_t*>(b_v + kLvMaxDims * kLvThreads);
+  uint32_t* sb = b_pos + kLvThreads;                      // [kLvSortCap]
+  uint16_t* b_key = reinterpret_cast<uint16_t*>(sb + kLvSortCap);  // [kLvThreads]
+  uint8_t* b_st = reinterpret_cast<uint8_t*>(b_key + kLvThreads);  // [kLvThreads]
+  uint8_t* w_st = b_st + kLvThreads;                      // [kLvWin]
+  uint8_t* e_st = w_st + kLvWin;                          // [kLvExt]
+  uint32_t* ctr = reinterpret_cast<uint32_t*>(
+      (reinterpret_cast<uintptr_t>(e_st + kLvExt) + 15) & ~uintptr_t(15));
+  // ctr: 0 window size, 1 extended size, 2 batch size, 3 overflow, 4 kept, 5 skyline kept
+
+  // 1. Counting sort of the survivors by cell sum.
+  for (uint32_t k = tid; k <= kLvKeyBins; k += blockDim.x) cur[k] = 0;
+  if (tid < 8) ctr[tid] = 0;
+  __syncthreads();
+  for (uint32_t i = tid; i < n; i += blockDim.x) atomicAdd(&cur[surv_key[off + i]], 1u);
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t acc = 0;
+    for (uint32_t k = 0; k < kLvKeyBins; ++k) {
+      kb[k] = acc;
+      acc += cur[k];
+    }
+    kb[kLvKeyBins] = acc;
+  }
+  __syncthreads();
+  for (uint32_t k = tid; k < kLvKeyBins; k += blockDim.x) cur[k] = kb[k];
+  __syncthreads();
+  for (uint32_t i = tid; i < n; i += blockDim.x) {
+    const uint32_t p = atomicAdd(&cur[surv_key[off + i]], 1u);
+    srt[off + p] = surv_id[off + i];
+  }
+  __syncthreads();
+
+  // 2. Sort-filter skyline in batches.
+  for (uint32_t base = 0; base < n; base += blockDim.x) {
+    const uint32_t i = base + tid;
+    const bool valid = i < n;
+    uint32_t pc = 0, key = 0;
+    float pv[kLvMaxDims];
+#pragma unroll
+    for (int a = 0; a < kLvMaxDims; ++a) pv[a] = 0.f;
+    int st = 2;
+    if (valid) {
+      const uint32_t id = srt[off + i];
+      pc = lv_pack(cells[id], A);
+      key = lv_key(pc);
+      lv_load(x, n_pad, id, A, pv);
+      st = 0;
+      const uint32_t wn = min(ctr[0], kLvWin);
+      for (uint32_t j = 0; j < wn; ++j) {
+        float qv[kLvMaxDims];
+#pragma unroll
+        for (int a = 0; a < kLvMaxDims; ++a) qv[a] = w_v[a * kLvWin + j];
+        const int r = lv_dom(w_c[j], qv, pc, pv, A);
+        if (r == 2) {
+          st = 2;
+          break;
+        }
+        if (r) st = 1;
+      }
+    }
+    __syncthreads();  // every thread has read ctr[0]
+    if (tid == 0) ctr[2] = 0;
+    __syncthreads();
+    if (st < 2) {
+      const uint32_t k = atomicAdd(&ctr[2], 1u);
+      b_c[k] = pc;
+#pragma unroll
+      for (int a = 0; a < kLvMaxDims; ++a) b_v[a * kLvThreads + k] = pv[a];
+      b_pos[k] = i;
+      b_key[k] = (uint16_t)key;
+      b_st[k] = (uint8_t)st;
+    }
+    __syncthreads();
+    const uint32_t nb = ctr[2];
+    int st2 = 2;
+    if ((uint32_t)tid < nb) {
+      st2 = b_st[tid];
+      pc = b_c[tid];
+      key = b_key[tid];
+#pragma unroll
+      for (int a = 0; a < kLvMaxDims; ++a) pv[a] = b_v[a * kLvThreads + tid];
+      for (uint32_t q = 0; q < nb; ++q) {
+        if (q == (uint32_t)tid || b_key[q] > key) continue;
+        float qv[kLvMaxDims];
+#pragma unroll
+        for (int a = 0; a < kLvMaxDims; ++a) qv[a] = b_v[a * kLvThreads + q];
+        const int r = lv_dom(b_c[q], qv, pc, pv, A);
+        if (r == 2) {
+          st2 = 2;
+          break;
+        }
+        if (r) st2 = 1;
+      }
+    }
+    __syncthreads();
+    if (st2 == 0) {
+      const uint32_t k = atomicAdd(&ctr[0], 1u);
+      if (k < kLvWin) {
+        w_c[k] = pc;
+#pragma unroll
+        for (int a = 0; a < kLvMaxDims; ++a) w_v[a * kLvWin + k] = pv[a];
+        w_pos[k] = b_pos[tid];
+        w_st[k] = 0;
+      } else {
+        ctr[3] = 1;
+      }
+    } else if (st2 == 1) {
+      const uint32_t k = atomicAdd(&ctr[1], 1u);
+      if (k < kLvExt) {
+        e_pos[k] = b_pos[tid];
+        e_st[k] = 1;
+      } else {
+        ctr[3] = 1;
+      }
+    }
+    __syncthreads();
+    if (ctr[3]) break;  // uniform: read after the barrier
+  }
+  if (ctr[3]) {
+    if (tid == 0) {
+      o_flag[c] = 1;
+      o_nsky[c] = 0;
+      o_next[c] = 0;
+    }
+    return;
+  }
+
+  // 3. Later entries of the same cell sum with equal cells on S.
+  const uint32_t wn = ctr[0], en = ctr[1], tot = wn + en;
+  for (uint32_t e = tid; e < tot; e += blockDim.x) {
+    const uint32_t pos = e < wn ? w_pos[e] : e_pos[e - wn];
+    int st = e < wn ? 0 : 1;
+    const uint32_t id = srt[off + pos];
+    const uint32_t pc = lv_pack(cells[id], A);
+    const uint32_t key = lv_key(pc);
+    float pv[kLvMaxDims];
+    bool have_v = false;
+    for (uint32_t j = kb[key]; j < kb[key + 1]; ++j) {
+      if (j == pos) continue;
+      const uint32_t qid = srt[off + j];
+      if (lv_pack(cells[qid], A) != pc) continue;
+      if (!have_v) {
+        lv_load(x, n_pad, id, A, pv);
+        have_v = true;
+      }
+      float qv[kLvMaxDims];
+      lv_load(x, n_pad, qid, A, qv);
+      const int r = lv_dom(pc, qv, pc, pv, A);
+      if (r == 2) {
+        st = 2;
+        break;
+      }
+      if (r) st = 1;
+    }
+    if (e < wn) w_st[e] = (uint8_t)st;
+    else e_st[e - wn] = (uint8_t)st;
+  }
+  __syncthreads();
+
+  // 4. Output: (status << 31 | id) sorted, so skyline ids come first, each
+  // part ascending.
+  for (uint32_t e = tid; e < tot; e += blockDim.x) {
+    const uint32_t pos = e < wn ? w_pos[e] : e_pos[e - wn];
+    const uint32_t st = e < wn ? w_st[e] : e_st[e - wn];
+    if (st < 2) {
+      const uint32_t k = atomicAdd(&ctr[4], 1u);
+      sb[k] = (st << 31) | srt[off + pos];
+      if (st == 0) atomicAdd(&ctr[5], 1u);
+    }
+  }
+  __syncthreads();
+  const uint32_t kept = ctr[4];
+  uint32_t p2 = 1;
+  while (p2 < kept) p2 <<= 1;
+  for (uint32_t k = kept + tid; k < p2; k += blockDim.x) sb[k] = 0xffffffffu;
+  __syncthreads();
+  for (uint32_t k = 2; k <= p2; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = tid; i < p2; i += blockDim.x) {
+        const uint32_t ixj = i ^ j;
+        if (ixj > i) {
+          const uint32_t a = sb[i], b = sb[ixj];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            sb[i] = b;
+            sb[ixj] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  const uint64_t so = (uint64_t)c * kLvSlot;
+  for (uint32_t k = tid; k < kept; k += blockDim.x) slot[so + k] = sb[k] & 0x7fffffffu;
+  if (tid == 0) {
+    o_nsky[c] = ctr[5];
+    o_next[c] = kept - ctr[5];
+    o_flag[c] = 0;
+  }
+}
+
+int launch_lv_filter(cudaStream_t s, const LvArgs& a) {
+  if (a.ncub == 0 || a.max_list == 0) return SKC_OK;
+  const dim3 grid(a.ncub, (unsigned)((a.max_list + kLvChunk - 1) / kLvChunk));
+  k_lv_filter<<<grid, 256, 0, s>>>(a.masks, a.lists, a.list_n, a.cells, a.x, a.n_pad, a.cap,
+                                   a.cnt, a.surv_id, a.surv_key);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
+int launch_lv_sfs(cudaStream_t s, const LvArgs& a) {
+  if (a.ncub == 0) return SKC_OK;
+  SKC_CUDA(cudaFuncSetAttribute(k_lv_sfs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kLvSfsSmem));
+  k_lv_sfs<<<a.ncub, kLvThreads, kLvSfsSmem, s>>>(a.masks, a.cells, a.x, a.n_pad, a.cap, a.cnt,
+                                                  a.surv_id, a.surv_key, a.srt, a.slot, a.o_nsky,
+                                                  a.o_next, a.o_flag);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
+}
+
+}  // namespace skc

@@ -72,6 +72,7 @@ def lib():
         "skc_dataset_free": (i32, [vp]),
         "skc_skycube": (i32, [vp, vp, P(_Options), P(vp)]),
         "skc_result_info": (i32, [vp, P(i32), P(u64), P(u64)]),
+        "skc_result_form": (i32, [vp, P(i32), P(i32)]),
         "skc_result_cuboid": (i32, [vp, u32, P(P(u32)), P(u64)]),
         "skc_result_extended": (i32, [vp, u32, P(P(u32)), P(u64)]),
         "skc_result_device_csr": (i32, [vp, P(vp), P(vp)]),
@@ -224,6 +225,15 @@ class Result:
         d, m, t = ctypes.c_int(), ctypes.c_uint64(), ctypes.c_uint64()
         _check(lib().skc_result_info(self.handle, ctypes.byref(d), ctypes.byref(m), ctypes.byref(t)))
         return {"d": d.value, "n_candidates": m.value, "total_skyline_ids": t.value}
+
+    FORMS = {1: "bitmaps", 2: "cuboids", 3: "levels", 4: "skyline"}
+
+    def form(self):
+        """(computation that produced the result, cuboids of the level form
+        that went through the per-cuboid pipeline)."""
+        f, fb = ctypes.c_int(), ctypes.c_int()
+        _check(lib().skc_result_form(self.handle, ctypes.byref(f), ctypes.byref(fb)))
+        return self.FORMS.get(f.value, "unknown"), fb.value
 
     def download(self):
         _check(lib().skc_result_download(self.handle))

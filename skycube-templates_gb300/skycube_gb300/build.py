@@ -23,7 +23,7 @@ CLI_PATH = os.path.join(BUILD, "skycube")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["api.cu", "prep.cu", "skyline.cu", "partition.cu", "mdmc.cu", "noalloc.cu",
-              "prefilter.cu"]
+              "prefilter.cu", "levels.cu"]
 
 
 def _nvcc():

@@ -1,0 +1,91 @@
+"""The level form of capped skycubes (max_d <= 4): every cuboid of a lattice
+level in one filter and one sort-filter launch, from its smallest computed
+parent. Checked against the C oracle on seeded inputs (each case asserts
+that the level form ran), on a tie-heavy input whose one-attribute skylines
+exceed the kernel's window (so the per-cuboid fallback runs), and against
+the bitmap form at sizes the oracle would take minutes on. Exact id-set
+equality per cuboid, skylines and extended skylines."""
+import numpy as np
+import pytest
+
+import oracle
+import skycube_gb300 as sk
+from skycube_gb300 import datagen
+
+pytestmark = pytest.mark.gpu
+
+
+def sets(r, d, max_d, ext=False):
+    out = {}
+    for c in range(1, 1 << d):
+        if bin(c).count("1") <= max_d or c == (1 << d) - 1:
+            out[c] = r.extended(c) if ext else r.cuboid(c)
+    return out
+
+
+def check(gpu_ctx, x, max_d, algos=("mdmc", "sdsc")):
+    d = x.shape[1]
+    sky, ext = oracle.stsc(x, max_d)
+    ds = sk.Dataset(gpu_ctx, x)
+    fallbacks = []
+    for algo in algos:
+        r = sk.skycube(gpu_ctx, ds, algo, "batched", max_d=max_d, want_extended=True)
+        form, fb = r.form()
+        assert form == "levels", form
+        fallbacks.append(fb)
+        got, gext = sets(r, d, max_d), sets(r, d, max_d, True)
+        for c in sky:
+            assert np.array_equal(got[c], sky[c]), f"{algo} skyline of cuboid {c}"
+            assert np.array_equal(gext[c], ext[c]), f"{algo} extended skyline of cuboid {c}"
+        r.close()
+    ds.close()
+    return fallbacks
+
+
+@pytest.mark.parametrize("kind,n,d,max_d,seed", [
+    ("anticorrelated", 12000, 6, 4, 3), ("anticorrelated", 12000, 8, 3, 3),
+    ("anticorrelated", 8000, 12, 4, 3), ("uniform", 20000, 10, 2, 3),
+    ("uniform", 20000, 14, 4, 3), ("anticorrelated", 6000, 16, 4, 3),
+    ("uniform", 20000, 10, 1, 4),
+])
+def test_levels_against_oracle(gpu_ctx, kind, n, d, max_d, seed):
+    check(gpu_ctx, datagen.generate(kind, n, d, seed), max_d)
+
+
+def test_levels_ties_and_fallback(gpu_ctx):
+    # Three values per attribute: about a third of the points share the
+    # minimum of each attribute, more than a level kernel's skyline window.
+    rng = np.random.default_rng(5)
+    x = np.floor(rng.random((12000, 6)) * 3).astype(np.float32)
+    fb = check(gpu_ctx, x, 2)
+    assert min(fb) >= 1
+
+
+def test_levels_duplicates_and_signed_zero(gpu_ctx):
+    base = datagen.generate("anticorrelated", 5000, 7, 6)
+    x = np.concatenate([base, base])
+    x[:40, 2] = -0.0
+    x[5000:5040, 2] = 0.0
+    check(gpu_ctx, x, 3)
+
+
+@pytest.mark.parametrize("kind,n,d,max_d,seed", [
+    ("anticorrelated", 500000, 16, 4, 1), ("uniform", 300000, 14, 3, 2),
+    ("anticorrelated", 400000, 10, 4, 93), ("correlated", 500000, 16, 4, 1),
+])
+def test_levels_equal_bitmap_form(gpu_ctx, kind, n, d, max_d, seed):
+    x = datagen.generate(kind, n, d, seed)
+    ds = sk.Dataset(gpu_ctx, x)
+    a = sk.skycube(gpu_ctx, ds, max_d=max_d, want_extended=True)
+    b = sk.skycube(gpu_ctx, ds, max_d=max_d, want_extended=True, want_bitmaps=True)
+    assert b.form()[0] == "bitmaps"
+    if a.info()["n_candidates"] >= 4096:
+        assert a.form()[0] == "levels"
+    for ext in (False, True):
+        sa, sb = sets(a, d, max_d, ext), sets(b, d, max_d, ext)
+        for c in sa:
+            assert np.array_equal(sa[c], sb[c]), f"cuboid {c} (extended={ext})"
+    assert a.info()["total_skyline_ids"] == b.info()["total_skyline_ids"]
+    a.close()
+    b.close()
+    ds.close()
