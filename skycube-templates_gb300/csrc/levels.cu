@@ -97,18 +97,51 @@ __device__ __forceinline__ int lv_dom(uint32_t qc, const float* qv, uint32_t pc,
 
 }  // namespace
 
+// The first kLvFirstPruners pruners are tested on every entry; the entries
+// they leave are staged and tested densely against the others, so a warp
+// runs the long pruner loop only on entries that need it.
+constexpr uint32_t kLvFirstPruners = 4;
+static constexpr size_t kLvFilterSmem = (size_t)kLvChunk * (4 + 4 + 4 + 2);
+
+// True when one of the pruners [j0, j1) strictly dominates p on S.
+__device__ __forceinline__ bool lv_pruned(uint32_t pc, uint32_t id, uint32_t j0, uint32_t j1,
+                                          const uint32_t* pr_c, const float (*pr_v)[kLvPruners],
+                                          const float* __restrict__ x, uint64_t n_pad,
+                                          const CubAttrs& A) {
+  float pv[kLvMaxDims];
+  bool have_v = false;
+  for (uint32_t j = j0; j < j1; ++j) {
+    const uint32_t qc = pr_c[j];
+    if ((ge_bytes(pc | kGuard, qc) & A.gm) != A.gm) continue;
+    const uint32_t eq = ge_bytes(qc | kGuard, pc) & A.gm;
+    if (!eq) return true;
+    if (!have_v) {
+      lv_load(x, n_pad, id, A, pv);
+      have_v = true;
+    }
+    bool strict = true;
+#pragma unroll
+    for (int a = 0; a < kLvMaxDims; ++a)
+      if ((eq & (0x80u << (8 * a))) && !(pr_v[a][j] < pv[a])) strict = false;
+    if (strict) return true;
+  }
+  return false;
+}
+
 __global__ void __launch_bounds__(256) k_lv_filter(
     const uint32_t* __restrict__ masks, const uint32_t* const* __restrict__ lists,
     const uint32_t* __restrict__ list_n, const uint4* __restrict__ cells,
     const float* __restrict__ x, uint64_t n_pad, uint32_t cap, uint32_t* __restrict__ cnt,
     uint32_t* __restrict__ surv_id, uint16_t* __restrict__ surv_key) {
   __shared__ uint32_t hist[kLvKeyBins];
-  __shared__ uint32_t s_thr, s_np, s_n, s_base;
+  __shared__ uint32_t s_thr, s_np, s_n1, s_n, s_base;
   __shared__ uint32_t pr_c[kLvPruners];
   __shared__ float pr_v[kLvMaxDims][kLvPruners];
-  // The chunk's survivors are staged here and appended with one atomic.
-  __shared__ uint32_t st_id[kLvChunk];
-  __shared__ uint16_t st_key[kLvChunk];
+  extern __shared__ __align__(16) unsigned char lvf_smem[];
+  uint32_t* s1_id = reinterpret_cast<uint32_t*>(lvf_smem);  // [kLvChunk] staged entries
+  uint32_t* s1_pc = s1_id + kLvChunk;                        // [kLvChunk]
+  uint32_t* st_id = s1_pc + kLvChunk;                        // [kLvChunk] survivors
+  uint16_t* st_key = reinterpret_cast<uint16_t*>(st_id + kLvChunk);  // [kLvChunk]
   // Consecutive CTAs take different cuboids, spreading the appends.
   const uint32_t c = blockIdx.x;
   const uint32_t n = list_n[c];
@@ -149,6 +182,7 @@ __global__ void __launch_bounds__(256) k_lv_filter(
     }
     s_thr = t;
     s_np = 0;
+    s_n1 = 0;
     s_n = 0;
   }
   __syncthreads();
@@ -171,47 +205,37 @@ __global__ void __launch_bounds__(256) k_lv_filter(
     __syncthreads();
   }
   const uint32_t np = min(s_np, kLvPruners);
+  const uint32_t np1 = min(np, kLvFirstPruners);
 
+  // Phase 1: every entry against the first pruners; the rest are staged.
   const uint32_t lt_mask = (1u << lane) - 1u;
   for (uint32_t base = beg; base < end; base += blockDim.x) {
     const uint32_t i = base + tid;
     const bool valid = i < end;
     uint32_t id = 0, pc = 0;
-    bool dead = false;
+    bool keep = false;
     if (valid) {
       id = L[i];
       pc = lv_pack(cells[id], A);
-      float pv[kLvMaxDims];
-      bool have_v = false;
-      for (uint32_t j = 0; j < np; ++j) {
-        const uint32_t qc = pr_c[j];
-        if ((ge_bytes(pc | kGuard, qc) & A.gm) != A.gm) continue;
-        const uint32_t eq = ge_bytes(qc | kGuard, pc) & A.gm;
-        if (!eq) {
-          dead = true;
-          break;
-        }
-        if (!have_v) {
-          lv_load(x, n_pad, id, A, pv);
-          have_v = true;
-        }
-        bool strict = true;
-#pragma unroll
-        for (int a = 0; a < kLvMaxDims; ++a)
-          if ((eq & (0x80u << (8 * a))) && !(pr_v[a][j] < pv[a])) strict = false;
-        if (strict) {
-          dead = true;
-          break;
-        }
-      }
+      keep = !lv_pruned(pc, id, 0, np1, pr_c, pr_v, x, n_pad, A);
     }
-    const bool keep = valid && !dead;
     const uint32_t live = __ballot_sync(kWarpAll, keep);
     uint32_t pos0 = 0;
-    if (lane == 0 && live) pos0 = atomicAdd(&s_n, (uint32_t)__popc(live));
+    if (lane == 0 && live) pos0 = atomicAdd(&s_n1, (uint32_t)__popc(live));
     pos0 = __shfl_sync(kWarpAll, pos0, 0);
     if (keep) {
       const uint32_t pos = pos0 + __popc(live & lt_mask);  // < kLvChunk
+      s1_id[pos] = id;
+      s1_pc[pos] = pc;
+    }
+  }
+  __syncthreads();
+  // Phase 2: the staged entries against the other pruners.
+  const uint32_t n1 = s_n1;
+  for (uint32_t k = tid; k < n1; k += blockDim.x) {
+    const uint32_t id = s1_id[k], pc = s1_pc[k];
+    if (!lv_pruned(pc, id, np1, np, pr_c, pr_v, x, n_pad, A)) {
+      const uint32_t pos = atomicAdd(&s_n, 1u);  // < kLvChunk
       st_id[pos] = id;
       st_key[pos] = (uint16_t)lv_key(pc);
     }
@@ -300,7 +324,12 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
   }
   __syncthreads();
 
-  // 2. Sort-filter skyline in batches.
+  // 2. Sort-filter skyline in batches of kLvThreads entries. The tests are
+  // warp-cooperative: a warp takes one entry at a time and its lanes test
+  // 32 window (or batch) entries per step, so no warp waits for its slowest
+  // lane's scan.
+  const int lane = tid & 31, wid = tid >> 5;
+  constexpr uint32_t kWarps = kLvThreads / 32;
   for (uint32_t base = 0; base < n; base += blockDim.x) {
     const uint32_t i = base + tid;
     const bool valid = i < n;
@@ -308,79 +337,102 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
     float pv[kLvMaxDims];
 #pragma unroll
     for (int a = 0; a < kLvMaxDims; ++a) pv[a] = 0.f;
-    int st = 2;
     if (valid) {
       const uint32_t id = srt[off + i];
       pc = lv_pack(cells[id], A);
       key = lv_key(pc);
       lv_load(x, n_pad, id, A, pv);
-      st = 0;
-      const uint32_t wn = min(ctr[0], kLvWin);
-      for (uint32_t j = 0; j < wn; ++j) {
-        float qv[kLvMaxDims];
+    }
+    // Window test of the warp's 32 entries, one entry per step.
+    const uint32_t wn = min(ctr[0], kLvWin);
+    int my_st = valid ? 0 : 2;
+    for (int e = 0; e < 32; ++e) {
+      if (!__shfl_sync(kWarpAll, (int)valid, e)) continue;
+      const uint32_t qpc = __shfl_sync(kWarpAll, pc, e);
+      float qpv[kLvMaxDims];
 #pragma unroll
-        for (int a = 0; a < kLvMaxDims; ++a) qv[a] = w_v[a * kLvWin + j];
-        const int r = lv_dom(w_c[j], qv, pc, pv, A);
-        if (r == 2) {
+      for (int a = 0; a < kLvMaxDims; ++a) qpv[a] = __shfl_sync(kWarpAll, pv[a], e);
+      int st = 0;
+      for (uint32_t j0 = 0; j0 < wn; j0 += 32) {
+        const uint32_t j = j0 + lane;
+        int r = 0;
+        if (j < wn) {
+          float wv[kLvMaxDims];
+#pragma unroll
+          for (int a = 0; a < kLvMaxDims; ++a) wv[a] = w_v[a * kLvWin + j];
+          r = lv_dom(w_c[j], wv, qpc, qpv, A);
+        }
+        if (__ballot_sync(kWarpAll, r == 2)) {
           st = 2;
           break;
         }
-        if (r) st = 1;
+        if (__ballot_sync(kWarpAll, r == 1)) st = 1;
       }
+      if (lane == e) my_st = st;
     }
     __syncthreads();  // every thread has read ctr[0]
     if (tid == 0) ctr[2] = 0;
     __syncthreads();
-    if (st < 2) {
+    if (my_st < 2) {
       const uint32_t k = atomicAdd(&ctr[2], 1u);
       b_c[k] = pc;
 #pragma unroll
       for (int a = 0; a < kLvMaxDims; ++a) b_v[a * kLvThreads + k] = pv[a];
       b_pos[k] = i;
       b_key[k] = (uint16_t)key;
-      b_st[k] = (uint8_t)st;
+      b_st[k] = (uint8_t)my_st;
     }
     __syncthreads();
+    // The batch's remaining entries against each other (only entries of a
+    // cell sum <= p's can dominate p); warp w takes entries w, w + 32, ...
     const uint32_t nb = ctr[2];
-    int st2 = 2;
-    if ((uint32_t)tid < nb) {
-      st2 = b_st[tid];
-      pc = b_c[tid];
-      key = b_key[tid];
+    for (uint32_t p = wid; p < nb; p += kWarps) {
+      const uint32_t ppc = b_c[p];
+      const uint32_t pkey = b_key[p];
+      float ppv[kLvMaxDims];
 #pragma unroll
-      for (int a = 0; a < kLvMaxDims; ++a) pv[a] = b_v[a * kLvThreads + tid];
-      for (uint32_t q = 0; q < nb; ++q) {
-        if (q == (uint32_t)tid || b_key[q] > key) continue;
-        float qv[kLvMaxDims];
+      for (int a = 0; a < kLvMaxDims; ++a) ppv[a] = b_v[a * kLvThreads + p];
+      int st = b_st[p];
+      for (uint32_t q0 = 0; q0 < nb; q0 += 32) {
+        const uint32_t q = q0 + lane;
+        int r = 0;
+        if (q < nb && q != p && b_key[q] <= pkey) {
+          float qv[kLvMaxDims];
 #pragma unroll
-        for (int a = 0; a < kLvMaxDims; ++a) qv[a] = b_v[a * kLvThreads + q];
-        const int r = lv_dom(b_c[q], qv, pc, pv, A);
-        if (r == 2) {
-          st2 = 2;
+          for (int a = 0; a < kLvMaxDims; ++a) qv[a] = b_v[a * kLvThreads + q];
+          r = lv_dom(b_c[q], qv, ppc, ppv, A);
+        }
+        if (__ballot_sync(kWarpAll, r == 2)) {
+          st = 2;
           break;
         }
-        if (r) st2 = 1;
+        if (__ballot_sync(kWarpAll, r == 1)) st = 1;
       }
+      __syncwarp();
+      if (lane == 0) b_st[p] = (uint8_t)st;  // only this warp reads b_st[p]
     }
     __syncthreads();
-    if (st2 == 0) {
-      const uint32_t k = atomicAdd(&ctr[0], 1u);
-      if (k < kLvWin) {
-        w_c[k] = pc;
+    if ((uint32_t)tid < nb) {
+      const int st2 = b_st[tid];
+      if (st2 == 0) {
+        const uint32_t k = atomicAdd(&ctr[0], 1u);
+        if (k < kLvWin) {
+          w_c[k] = b_c[tid];
 #pragma unroll
-        for (int a = 0; a < kLvMaxDims; ++a) w_v[a * kLvWin + k] = pv[a];
-        w_pos[k] = b_pos[tid];
-        w_st[k] = 0;
-      } else {
-        ctr[3] = 1;
-      }
-    } else if (st2 == 1) {
-      const uint32_t k = atomicAdd(&ctr[1], 1u);
-      if (k < kLvExt) {
-        e_pos[k] = b_pos[tid];
-        e_st[k] = 1;
-      } else {
-        ctr[3] = 1;
+          for (int a = 0; a < kLvMaxDims; ++a) w_v[a * kLvWin + k] = b_v[a * kLvThreads + tid];
+          w_pos[k] = b_pos[tid];
+          w_st[k] = 0;
+        } else {
+          ctr[3] = 1;
+        }
+      } else if (st2 == 1) {
+        const uint32_t k = atomicAdd(&ctr[1], 1u);
+        if (k < kLvExt) {
+          e_pos[k] = b_pos[tid];
+          e_st[k] = 1;
+        } else {
+          ctr[3] = 1;
+        }
       }
     }
     __syncthreads();
@@ -395,35 +447,39 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
     return;
   }
 
-  // 3. Later entries of the same cell sum with equal cells on S.
+  // 3. Later entries of the same cell sum with equal cells on S; a warp per
+  // skyline or extended entry, its lanes over the bucket.
   const uint32_t wn = ctr[0], en = ctr[1], tot = wn + en;
-  for (uint32_t e = tid; e < tot; e += blockDim.x) {
+  for (uint32_t e = wid; e < tot; e += kWarps) {
     const uint32_t pos = e < wn ? w_pos[e] : e_pos[e - wn];
     int st = e < wn ? 0 : 1;
     const uint32_t id = srt[off + pos];
     const uint32_t pc = lv_pack(cells[id], A);
     const uint32_t key = lv_key(pc);
     float pv[kLvMaxDims];
-    bool have_v = false;
-    for (uint32_t j = kb[key]; j < kb[key + 1]; ++j) {
-      if (j == pos) continue;
-      const uint32_t qid = srt[off + j];
-      if (lv_pack(cells[qid], A) != pc) continue;
-      if (!have_v) {
-        lv_load(x, n_pad, id, A, pv);
-        have_v = true;
+    lv_load(x, n_pad, id, A, pv);
+    const uint32_t j1 = kb[key + 1];
+    for (uint32_t j0 = kb[key]; j0 < j1; j0 += 32) {
+      const uint32_t j = j0 + lane;
+      int r = 0;
+      if (j < j1 && j != pos) {
+        const uint32_t qid = srt[off + j];
+        if (lv_pack(cells[qid], A) == pc) {
+          float qv[kLvMaxDims];
+          lv_load(x, n_pad, qid, A, qv);
+          r = lv_dom(pc, qv, pc, pv, A);
+        }
       }
-      float qv[kLvMaxDims];
-      lv_load(x, n_pad, qid, A, qv);
-      const int r = lv_dom(pc, qv, pc, pv, A);
-      if (r == 2) {
+      if (__ballot_sync(kWarpAll, r == 2)) {
         st = 2;
         break;
       }
-      if (r) st = 1;
+      if (__ballot_sync(kWarpAll, r == 1)) st = 1;
     }
-    if (e < wn) w_st[e] = (uint8_t)st;
-    else e_st[e - wn] = (uint8_t)st;
+    if (lane == 0) {
+      if (e < wn) w_st[e] = (uint8_t)st;
+      else e_st[e - wn] = (uint8_t)st;
+    }
   }
   __syncthreads();
 
@@ -472,7 +528,9 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
 int launch_lv_filter(cudaStream_t s, const LvArgs& a) {
   if (a.ncub == 0 || a.max_list == 0) return SKC_OK;
   const dim3 grid(a.ncub, (unsigned)((a.max_list + kLvChunk - 1) / kLvChunk));
-  k_lv_filter<<<grid, 256, 0, s>>>(a.masks, a.lists, a.list_n, a.cells, a.x, a.n_pad, a.cap,
+  SKC_CUDA(cudaFuncSetAttribute(k_lv_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kLvFilterSmem));
+  k_lv_filter<<<grid, 256, kLvFilterSmem, s>>>(a.masks, a.lists, a.list_n, a.cells, a.x, a.n_pad, a.cap,
                                    a.cnt, a.surv_id, a.surv_key);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
