@@ -100,6 +100,11 @@ typedef struct skc_options {
                         grab, 1..64; 0 auto (1) */
   int blocks_per_sm; /* bitmap kernel: persistent CTAs per SM, 1..32 (capped
                         by occupancy); 0 auto (the occupancy limit) */
+  int form;          /* computation of a batched skycube (SKC_FORM_*): 0 auto;
+                        SKC_FORM_BITMAPS; SKC_FORM_LEVELS where it applies
+                        (max_d <= 4 and <= d - 2, no per-point bitmaps; it
+                        hands over to the bitmaps when too many cuboids
+                        exceed its capacities). Never changes the result */
 } skc_options;
 
 /* Fills *opt with defaults: MDMC, BATCHED, all cuboids, automatic work

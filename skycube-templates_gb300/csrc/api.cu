@@ -712,6 +712,11 @@ static int run_sdsc_plain(Exec& E, skc_dataset* ds, int max_d,
 // kernel's capacities go through the single-cuboid pipeline.
 constexpr uint64_t kLvScratchBytes = 2048ull << 20;  // survivor scratch per group
 constexpr uint32_t kLvMaxSurvivors = 262144;         // per cuboid
+// More cuboids over the capacities than this on the first level (heavy
+// exact ties: the per-cuboid fallback would dominate) and the bitmap form
+// takes over; run_levels then returns kLvGiveUp with the result untouched.
+constexpr int kLvMaxFallbacks = 16;
+constexpr int kLvGiveUp = 1000;
 
 static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d, int depth,
                       Arena& A, FullSpace& F, skc_result* R, Tracer& T) {
@@ -731,6 +736,17 @@ static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d,
   CuboidScratch cs;
   bool cs_ready = false;
   int fallbacks = 0;
+  // Cells on a grid of the candidates' own quantiles, by point id: on the
+  // full-space grid most candidates of correlated data share one cell on
+  // every attribute, which leaves the cell sums no order to give.
+  const uint64_t m = F.h_counts[2];
+  float* pivots;
+  uint4 *cc, *lv_cells;
+  SKC_TRY(A.alloc(&pivots, (uint64_t)kMaxDims * kMaxPivots));
+  SKC_TRY(A.alloc(&cc, m));
+  SKC_TRY(A.alloc(&lv_cells, ds->n));
+  SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, F.cand, F.counts + 2, m, depth, pivots, cc));
+  SKC_TRY(launch_scatter_u4(s, cc, F.cand, F.counts + 2, m, lv_cells));
 
   for (int lev = max_d; lev >= 1; --lev) {
     std::vector<uint32_t> cubs;
@@ -767,7 +783,7 @@ static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d,
     for (uint32_t g0 = 0; g0 < nc; g0 += G) {
       const uint32_t ng = std::min(G, nc - g0);
       SKC_CUDA(cudaMemsetAsync(cnt, 0, ng * sizeof(uint32_t), s));
-      LvArgs a{ng, d_masks + g0, d_lists + g0, d_n + g0, (uint32_t)maxn, F.cells, ds->x,
+      LvArgs a{ng, d_masks + g0, d_lists + g0, d_n + g0, (uint32_t)maxn, lv_cells, ds->x,
                ds->n_pad, cap, cnt, surv_id, surv_key, srt, slot + (uint64_t)g0 * kLvSlot,
                outs + g0, outs + nc + g0, outs + 2ull * nc + g0};
       SKC_TRY(launch_lv_filter(s, a));
@@ -776,6 +792,11 @@ static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d,
     std::vector<uint32_t> h(3ull * nc);
     SKC_CUDA(cudaMemcpyAsync(h.data(), outs, 3ull * nc * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     SKC_CUDA(cudaStreamSynchronize(s));  // also keeps the uploaded host vectors alive
+    if (lev == max_d) {
+      int over = 0;
+      for (uint32_t i = 0; i < nc; ++i) over += h[2ull * nc + i] != 0;
+      if (over > kLvMaxFallbacks) return kLvGiveUp;
+    }
     for (uint32_t i = 0; i < nc; ++i) {
       const uint32_t c = cubs[i];
       if (h[2ull * nc + i] == 0) {
@@ -816,15 +837,19 @@ static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d,
 }
 
 // The level form replaces the bitmaps for batched capped skycubes of small
-// caps on enough candidates (below that the bitmap kernel is as fast), when
-// no per-point bitmaps are wanted and no plan is being recorded (the level
-// form syncs per level).
-constexpr uint64_t kLvMinCandidates = 4096;
+// caps on many candidates, when no per-point bitmaps are wanted and no plan
+// is being recorded (the level form syncs per level). Below 65,536
+// candidates the bitmap kernel is as fast or faster, and tie-heavy data
+// (whose small cuboids have skylines over the level kernels' capacities)
+// has few candidates.
+constexpr uint64_t kLvMinCandidates = 65536;
 static bool use_levels(const Exec& E, const skc_dataset* ds, const skc_options& o, int max_d,
                        const FullSpace& F) {
-  return !E.plan && o.mode == SKC_MODE_BATCHED && !o.want_bitmaps && max_d <= kLvMaxDims &&
-         max_d <= ds->d - 2 && F.h_counts[2] >= kLvMinCandidates && ds->n < (1ull << 31) &&
-         F.h_counts[2] <= 65535ull * kLvChunk;  // filter grid's y extent
+  if (o.form == SKC_FORM_BITMAPS) return false;
+  const bool can = !E.plan && o.mode == SKC_MODE_BATCHED && !o.want_bitmaps &&
+                   max_d <= kLvMaxDims && max_d <= ds->d - 2 && ds->n < (1ull << 31) &&
+                   F.h_counts[2] <= 65535ull * kLvChunk;  // filter grid's y extent
+  return can && (o.form == SKC_FORM_LEVELS || F.h_counts[2] >= kLvMinCandidates);
 }
 
 static int auto_depth(uint64_t n, int d) {
@@ -1066,6 +1091,7 @@ void skc_options_init(skc_options* o) {
   o->tile_points = 0;
   o->chunk = 0;
   o->blocks_per_sm = 0;
+  o->form = 0;
 }
 
 int skc_context_create(int device, skc_context** out) {
@@ -1223,6 +1249,9 @@ static int check_options(skc_dataset* ds, const skc_options* opt, skc_options* o
   if (o->blocks_per_sm < 0 || o->blocks_per_sm > 32)
     return set_error(SKC_ERR_INVALID, "blocks_per_sm %d outside [1, 32] (0 = auto)",
                      o->blocks_per_sm);
+  if (o->form != 0 && o->form != SKC_FORM_BITMAPS && o->form != SKC_FORM_LEVELS)
+    return set_error(SKC_ERR_INVALID, "form %d is not 0, SKC_FORM_BITMAPS or SKC_FORM_LEVELS",
+                     o->form);
   return SKC_OK;
 }
 
@@ -1370,6 +1399,10 @@ static int skycube_exec(Exec& E, skc_dataset* ds, const skc_options* opt, skc_re
       } else if (use_levels(E, ds, o, max_d, F)) {
         R->form = SKC_FORM_LEVELS;
         st = run_levels(E, ds, o, max_d, depth, A, F, R, T);
+        if (st == kLvGiveUp) {
+          R->form = SKC_FORM_BITMAPS;
+          st = run_bitmaps(E, ds, o, P, max_d, A, F, R, T);
+        }
       } else {
         R->form = SKC_FORM_BITMAPS;
         st = run_bitmaps(E, ds, o, P, max_d, A, F, R, T);

@@ -250,6 +250,8 @@ struct LvArgs {
   uint32_t* o_flag;              // [ncub] 1: over a capacity, not computed
 };
 int launch_lv_filter(cudaStream_t s, const LvArgs& a);
+int launch_scatter_u4(cudaStream_t s, const uint4* in, const uint32_t* idx, const uint32_t* m_ptr,
+                      uint64_t m_max, uint4* out);
 int launch_lv_sfs(cudaStream_t s, const LvArgs& a);
 
 void upload_submask_table();

@@ -299,7 +299,8 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
   uint8_t* e_st = w_st + kLvWin;                          // [kLvExt]
   uint32_t* ctr = reinterpret_cast<uint32_t*>(
       (reinterpret_cast<uintptr_t>(e_st + kLvExt) + 15) & ~uintptr_t(15));
-  // ctr: 0 window size, 1 extended size, 2 batch size, 3 overflow, 4 kept, 5 skyline kept
+  // ctr: 0 window size, 1 extended size, 2 batch size, 3 overflow, 4 kept,
+  // 5 skyline kept, 6 end of the current batch
 
   // 1. Counting sort of the survivors by cell sum.
   for (uint32_t k = tid; k <= kLvKeyBins; k += blockDim.x) cur[k] = 0;
@@ -328,11 +329,29 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
   // warp-cooperative: a warp takes one entry at a time and its lanes test
   // 32 window (or batch) entries per step, so no warp waits for its slowest
   // lane's scan.
+  // A batch ends on a cell-sum bucket boundary when one lies in its range,
+  // so entries of equal sum (which may dominate each other in either order)
+  // meet in the same batch; only buckets larger than a batch are split.
   const int lane = tid & 31, wid = tid >> 5;
   constexpr uint32_t kWarps = kLvThreads / 32;
-  for (uint32_t base = 0; base < n; base += blockDim.x) {
+  for (uint32_t base = 0, bend = 0; base < n; base = bend) {
+    if (tid == 0) {
+      const uint32_t target = base + kLvThreads;
+      uint32_t e = n;
+      if (target < n) {
+        uint32_t lo = 0, hi = kLvKeyBins;  // largest k with kb[k] <= target
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi + 1) >> 1;
+          if (kb[mid] <= target) lo = mid; else hi = mid - 1;
+        }
+        e = kb[lo] > base ? kb[lo] : target;
+      }
+      ctr[6] = e;
+    }
+    __syncthreads();
+    bend = ctr[6];
     const uint32_t i = base + tid;
-    const bool valid = i < n;
+    const bool valid = i < bend;
     uint32_t pc = 0, key = 0;
     float pv[kLvMaxDims];
 #pragma unroll
@@ -523,6 +542,24 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
     o_next[c] = kept - ctr[5];
     o_flag[c] = 0;
   }
+}
+
+// out[idx[i]] = in[i] for i < *m_ptr.
+__global__ void k_scatter_u4(const uint4* __restrict__ in, const uint32_t* __restrict__ idx,
+                             const uint32_t* __restrict__ m_ptr, uint4* __restrict__ out) {
+  const uint32_t m = *m_ptr;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+    out[idx[i]] = in[i];
+}
+
+int launch_scatter_u4(cudaStream_t s, const uint4* in, const uint32_t* idx, const uint32_t* m_ptr,
+                      uint64_t m_max, uint4* out) {
+  uint64_t b = (m_max + 255) / 256;
+  if (b < 1) b = 1;
+  if (b > 152 * 8) b = 152 * 8;
+  k_scatter_u4<<<(unsigned)b, 256, 0, s>>>(in, idx, m_ptr, out);
+  SKC_LAUNCH_CHECK();
+  return SKC_OK;
 }
 
 int launch_lv_filter(cudaStream_t s, const LvArgs& a) {

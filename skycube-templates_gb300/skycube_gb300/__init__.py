@@ -43,7 +43,8 @@ class _Options(ctypes.Structure):
                 ("depth", ctypes.c_int), ("want_extended", ctypes.c_int),
                 ("want_bitmaps", ctypes.c_int), ("subspace", ctypes.c_uint32),
                 ("pq_size", ctypes.c_int), ("tile_points", ctypes.c_int),
-                ("chunk", ctypes.c_int), ("blocks_per_sm", ctypes.c_int)]
+                ("chunk", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
+                ("form", ctypes.c_int)]
 
     def work_params(self):
         return {"depth": self.depth, "pq_size": self.pq_size, "tile_points": self.tile_points,
@@ -286,25 +287,30 @@ def kernel_launches():
     return int(lib().skc_kernel_launches())
 
 
+FORM_CODES = {"auto": 0, "bitmaps": 1, "levels": 3}
+
+
 def options(algo="mdmc", mode="batched", max_d=0, depth=0, want_extended=False,
             want_bitmaps=False, subspace=0, pq_size=0, tile_points=0, chunk=0,
-            blocks_per_sm=0):
+            blocks_per_sm=0, form="auto"):
     """skc_options. The work parameters (depth, pq_size, tile_points, chunk,
     blocks_per_sm) change the work, never the result; 0 = automatic (a stored
     tuning for datasets like this one, else the default); pq_size < 0 turns
-    the prefilter off."""
+    the prefilter off. form: "auto", "bitmaps" or "levels" (the computation
+    of a batched capped skycube; never changes the result)."""
     return _Options(ALGOS[algo], MODES[mode], int(max_d), int(depth),
                     int(bool(want_extended)), int(bool(want_bitmaps)), int(subspace),
-                    int(pq_size), int(tile_points), int(chunk), int(blocks_per_sm))
+                    int(pq_size), int(tile_points), int(chunk), int(blocks_per_sm),
+                    FORM_CODES[form])
 
 
 def skycube(ctx, ds, algo="mdmc", mode="batched", max_d=0, depth=0,
             want_extended=False, want_bitmaps=False, subspace=0, pq_size=0,
-            tile_points=0, chunk=0, blocks_per_sm=0):
+            tile_points=0, chunk=0, blocks_per_sm=0, form="auto"):
     """Computes the skycube of a resident dataset (MDMC/SDSC ::Execute), or
     with `subspace` set, only that cuboid's skyline (a skyline query)."""
     o = options(algo, mode, max_d, depth, want_extended, want_bitmaps, subspace, pq_size,
-                tile_points, chunk, blocks_per_sm)
+                tile_points, chunk, blocks_per_sm, form)
     h = ctypes.c_void_p()
     _check(lib().skc_skycube(ctx.handle, ds.handle, ctypes.byref(o), ctypes.byref(h)))
     md = ds.d if max_d <= 0 or max_d > ds.d else max_d

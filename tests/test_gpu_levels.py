@@ -1,7 +1,7 @@
 """The level form of capped skycubes (max_d <= 4): every cuboid of a lattice
 level in one filter and one sort-filter launch, from its smallest computed
-parent. Checked against the C oracle on seeded inputs (each case asserts
-that the level form ran), on a tie-heavy input whose one-attribute skylines
+parent. Checked against the C oracle on seeded inputs (the form forced,
+each case asserting that it ran), on a tie-heavy input whose one-attribute skylines
 exceed the kernel's window (so the per-cuboid fallback runs), and against
 the bitmap form at sizes the oracle would take minutes on. Exact id-set
 equality per cuboid, skylines and extended skylines."""
@@ -29,7 +29,8 @@ def check(gpu_ctx, x, max_d, algos=("mdmc", "sdsc")):
     ds = sk.Dataset(gpu_ctx, x)
     fallbacks = []
     for algo in algos:
-        r = sk.skycube(gpu_ctx, ds, algo, "batched", max_d=max_d, want_extended=True)
+        r = sk.skycube(gpu_ctx, ds, algo, "batched", max_d=max_d, want_extended=True,
+                       form="levels")
         form, fb = r.form()
         assert form == "levels", form
         fallbacks.append(fb)
@@ -61,6 +62,25 @@ def test_levels_ties_and_fallback(gpu_ctx):
     assert min(fb) >= 1
 
 
+def test_levels_give_up_to_bitmaps(gpu_ctx):
+    # Two values per attribute: every 2-attribute skyline holds about a
+    # quarter of the points, over the window on every top-level cuboid, so
+    # the level form hands over and the bitmap form computes the result.
+    rng = np.random.default_rng(7)
+    x = np.floor(rng.random((20000, 8)) * 2).astype(np.float32)
+    d, m = 8, 2
+    sky, ext = oracle.stsc(x, m)
+    ds = sk.Dataset(gpu_ctx, x)
+    r = sk.skycube(gpu_ctx, ds, max_d=m, want_extended=True, form="levels")
+    assert r.form()[0] == "bitmaps"
+    got, gext = sets(r, d, m), sets(r, d, m, True)
+    for c in sky:
+        assert np.array_equal(got[c], sky[c]), f"skyline of cuboid {c}"
+        assert np.array_equal(gext[c], ext[c]), f"extended skyline of cuboid {c}"
+    r.close()
+    ds.close()
+
+
 def test_levels_duplicates_and_signed_zero(gpu_ctx):
     base = datagen.generate("anticorrelated", 5000, 7, 6)
     x = np.concatenate([base, base])
@@ -77,9 +97,9 @@ def test_levels_equal_bitmap_form(gpu_ctx, kind, n, d, max_d, seed):
     x = datagen.generate(kind, n, d, seed)
     ds = sk.Dataset(gpu_ctx, x)
     a = sk.skycube(gpu_ctx, ds, max_d=max_d, want_extended=True)
-    b = sk.skycube(gpu_ctx, ds, max_d=max_d, want_extended=True, want_bitmaps=True)
+    b = sk.skycube(gpu_ctx, ds, max_d=max_d, want_extended=True, form="bitmaps")
     assert b.form()[0] == "bitmaps"
-    if a.info()["n_candidates"] >= 4096:
+    if a.info()["n_candidates"] >= 65536:
         assert a.form()[0] == "levels"
     for ext in (False, True):
         sa, sb = sets(a, d, max_d, ext), sets(b, d, max_d, ext)
