@@ -777,6 +777,11 @@ static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d,
     SKC_TRY(A.alloc(&surv_id, (uint64_t)G * cap));
     SKC_TRY(A.alloc(&surv_key, (uint64_t)G * cap));
     SKC_TRY(A.alloc(&srt, (uint64_t)G * cap));
+    uint32_t *pr_c, *pr_n;
+    float* pr_v;
+    SKC_TRY(A.alloc(&pr_c, (uint64_t)G * kLvPruners));
+    SKC_TRY(A.alloc(&pr_v, (uint64_t)G * kLvMaxDims * kLvPruners));
+    SKC_TRY(A.alloc(&pr_n, G));
     SKC_CUDA(cudaMemcpyAsync(d_masks, cubs.data(), nc * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     SKC_CUDA(cudaMemcpyAsync(d_n, hn.data(), nc * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     SKC_CUDA(cudaMemcpyAsync(d_lists, hl.data(), nc * sizeof(void*), cudaMemcpyHostToDevice, s));
@@ -784,7 +789,8 @@ static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d,
       const uint32_t ng = std::min(G, nc - g0);
       SKC_CUDA(cudaMemsetAsync(cnt, 0, ng * sizeof(uint32_t), s));
       LvArgs a{ng, d_masks + g0, d_lists + g0, d_n + g0, (uint32_t)maxn, lv_cells, ds->x,
-               ds->n_pad, cap, cnt, surv_id, surv_key, srt, slot + (uint64_t)g0 * kLvSlot,
+               ds->n_pad, pr_c, pr_v, pr_n, cap, cnt, surv_id, surv_key, srt,
+               slot + (uint64_t)g0 * kLvSlot,
                outs + g0, outs + nc + g0, outs + 2ull * nc + g0};
       SKC_TRY(launch_lv_filter(s, a));
       SKC_TRY(launch_lv_sfs(s, a));

@@ -239,6 +239,9 @@ struct LvArgs {
   const uint4* cells;            // point id -> grid cells
   const float* x;                // attribute-major points, pitch n_pad
   uint64_t n_pad;
+  uint32_t* pr_c;                // [ncub * kLvPruners] pruner cells (packed over S)
+  float* pr_v;                   // [ncub * kLvMaxDims * kLvPruners] pruner values
+  uint32_t* pr_n;                // [ncub] pruners per cuboid
   uint32_t cap;                  // survivors kept per cuboid
   uint32_t* cnt;                 // [ncub] survivors (zeroed before the filter)
   uint32_t* surv_id;             // [ncub * cap]

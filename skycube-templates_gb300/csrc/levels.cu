@@ -128,32 +128,24 @@ __device__ __forceinline__ bool lv_pruned(uint32_t pc, uint32_t id, uint32_t j0,
   return false;
 }
 
-__global__ void __launch_bounds__(256) k_lv_filter(
+// Pruners of each cuboid: the lowest cell sums over S of a strided sample
+// of its list, selected once per cuboid for all its filter CTAs.
+__global__ void __launch_bounds__(256) k_lv_pruners(
     const uint32_t* __restrict__ masks, const uint32_t* const* __restrict__ lists,
     const uint32_t* __restrict__ list_n, const uint4* __restrict__ cells,
-    const float* __restrict__ x, uint64_t n_pad, uint32_t cap, uint32_t* __restrict__ cnt,
-    uint32_t* __restrict__ surv_id, uint16_t* __restrict__ surv_key) {
+    const float* __restrict__ x, uint64_t n_pad, uint32_t* __restrict__ pr_c_g,
+    float* __restrict__ pr_v_g, uint32_t* __restrict__ pr_n_g) {
   __shared__ uint32_t hist[kLvKeyBins];
-  __shared__ uint32_t s_thr, s_np, s_n1, s_n, s_base;
-  __shared__ uint32_t pr_c[kLvPruners];
-  __shared__ float pr_v[kLvMaxDims][kLvPruners];
-  extern __shared__ __align__(16) unsigned char lvf_smem[];
-  uint32_t* s1_id = reinterpret_cast<uint32_t*>(lvf_smem);  // [kLvChunk] staged entries
-  uint32_t* s1_pc = s1_id + kLvChunk;                        // [kLvChunk]
-  uint32_t* st_id = s1_pc + kLvChunk;                        // [kLvChunk] survivors
-  uint16_t* st_key = reinterpret_cast<uint16_t*>(st_id + kLvChunk);  // [kLvChunk]
-  // Consecutive CTAs take different cuboids, spreading the appends.
+  __shared__ uint32_t s_thr, s_np;
   const uint32_t c = blockIdx.x;
   const uint32_t n = list_n[c];
-  const uint32_t beg = blockIdx.y * kLvChunk;
-  if (beg >= n) return;  // uniform over the CTA
-  const uint32_t end = min(n, beg + kLvChunk);
+  const int tid = threadIdx.x;
+  if (n == 0) {  // uniform over the CTA
+    if (tid == 0) pr_n_g[c] = 0;
+    return;
+  }
   const uint32_t* __restrict__ L = lists[c];
   const CubAttrs A = cub_attrs(masks[c]);
-  const int tid = threadIdx.x, lane = tid & 31;
-
-  // Pruners: the lowest cell sums of a strided sample (every CTA of the
-  // cuboid picks the same ones).
   const uint32_t ns = min(n, kLvSample);
   for (uint32_t i = tid; i < kLvKeyBins; i += blockDim.x) hist[i] = 0;
   __syncthreads();
@@ -182,8 +174,6 @@ __global__ void __launch_bounds__(256) k_lv_filter(
     }
     s_thr = t;
     s_np = 0;
-    s_n1 = 0;
-    s_n = 0;
   }
   __syncthreads();
   const uint32_t thr = s_thr;
@@ -194,17 +184,55 @@ __global__ void __launch_bounds__(256) k_lv_filter(
       if (take) {
         const uint32_t k = atomicAdd(&s_np, 1u);
         if (k < kLvPruners) {
-          pr_c[k] = lv_pack(cells[sid[r]], A);
+          pr_c_g[(uint64_t)c * kLvPruners + k] = lv_pack(cells[sid[r]], A);
           float v[kLvMaxDims];
           lv_load(x, n_pad, sid[r], A, v);
 #pragma unroll
-          for (int a = 0; a < kLvMaxDims; ++a) pr_v[a][k] = v[a];
+          for (int a = 0; a < kLvMaxDims; ++a)
+            pr_v_g[((uint64_t)c * kLvMaxDims + a) * kLvPruners + k] = v[a];
         }
       }
     }
     __syncthreads();
   }
-  const uint32_t np = min(s_np, kLvPruners);
+  if (tid == 0) pr_n_g[c] = min(s_np, kLvPruners);
+}
+
+__global__ void __launch_bounds__(256) k_lv_filter(
+    const uint32_t* __restrict__ masks, const uint32_t* const* __restrict__ lists,
+    const uint32_t* __restrict__ list_n, const uint4* __restrict__ cells,
+    const float* __restrict__ x, uint64_t n_pad, const uint32_t* __restrict__ pr_c_g,
+    const float* __restrict__ pr_v_g, const uint32_t* __restrict__ pr_n_g, uint32_t cap,
+    uint32_t* __restrict__ cnt, uint32_t* __restrict__ surv_id, uint16_t* __restrict__ surv_key) {
+  __shared__ uint32_t s_n1, s_n, s_base;
+  __shared__ uint32_t pr_c[kLvPruners];
+  __shared__ float pr_v[kLvMaxDims][kLvPruners];
+  extern __shared__ __align__(16) unsigned char lvf_smem[];
+  uint32_t* s1_id = reinterpret_cast<uint32_t*>(lvf_smem);  // [kLvChunk] staged entries
+  uint32_t* s1_pc = s1_id + kLvChunk;                        // [kLvChunk]
+  uint32_t* st_id = s1_pc + kLvChunk;                        // [kLvChunk] survivors
+  uint16_t* st_key = reinterpret_cast<uint16_t*>(st_id + kLvChunk);  // [kLvChunk]
+  // Consecutive CTAs take different cuboids, spreading the appends.
+  const uint32_t c = blockIdx.x;
+  const uint32_t n = list_n[c];
+  const uint32_t beg = blockIdx.y * kLvChunk;
+  if (beg >= n) return;  // uniform over the CTA
+  const uint32_t end = min(n, beg + kLvChunk);
+  const uint32_t* __restrict__ L = lists[c];
+  const CubAttrs A = cub_attrs(masks[c]);
+  const int tid = threadIdx.x, lane = tid & 31;
+  if (tid < (int)kLvPruners) {
+    pr_c[tid] = pr_c_g[(uint64_t)c * kLvPruners + tid];
+#pragma unroll
+    for (int a = 0; a < kLvMaxDims; ++a)
+      pr_v[a][tid] = pr_v_g[((uint64_t)c * kLvMaxDims + a) * kLvPruners + tid];
+  }
+  if (tid == 0) {
+    s_n1 = 0;
+    s_n = 0;
+  }
+  __syncthreads();
+  const uint32_t np = pr_n_g[c];
   const uint32_t np1 = min(np, kLvFirstPruners);
 
   // Phase 1: every entry against the first pruners; the rest are staged.
@@ -565,10 +593,14 @@ int launch_scatter_u4(cudaStream_t s, const uint4* in, const uint32_t* idx, cons
 int launch_lv_filter(cudaStream_t s, const LvArgs& a) {
   if (a.ncub == 0 || a.max_list == 0) return SKC_OK;
   const dim3 grid(a.ncub, (unsigned)((a.max_list + kLvChunk - 1) / kLvChunk));
+  k_lv_pruners<<<a.ncub, 256, 0, s>>>(a.masks, a.lists, a.list_n, a.cells, a.x, a.n_pad,
+                                      a.pr_c, a.pr_v, a.pr_n);
+  SKC_LAUNCH_CHECK();
   SKC_CUDA(cudaFuncSetAttribute(k_lv_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kLvFilterSmem));
-  k_lv_filter<<<grid, 256, kLvFilterSmem, s>>>(a.masks, a.lists, a.list_n, a.cells, a.x, a.n_pad, a.cap,
-                                   a.cnt, a.surv_id, a.surv_key);
+  k_lv_filter<<<grid, 256, kLvFilterSmem, s>>>(a.masks, a.lists, a.list_n, a.cells, a.x, a.n_pad,
+                                               a.pr_c, a.pr_v, a.pr_n, a.cap, a.cnt, a.surv_id,
+                                               a.surv_key);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }
