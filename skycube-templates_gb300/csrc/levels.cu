@@ -8,11 +8,12 @@
 // kLvMaxDims attributes.
 //
 // Per cuboid S and candidate list L:
-//  1. k_lv_filter: 32 pruners = the lowest cell sums over S of a 1,024-entry
-//     strided sample of L; every entry of L that a pruner strictly dominates
-//     on S is dropped (exact float test on equal cells). If a dropped q
-//     dominated a kept p, the pruner that drops q would strictly dominate p,
-//     so the kept entries (survivors) decide each other's status alone.
+//  1. k_lv_pruners: 32 pruners = the lowest cell sums over S of a
+//     1,024-entry strided sample of L. k_lv_filter: every entry of L that a
+//     pruner strictly dominates on S is dropped (exact float test on equal
+//     cells). If a dropped q dominated a kept p, the pruner that drops q
+//     would strictly dominate p, so the kept entries (survivors) decide each
+//     other's status alone.
 //  2. k_lv_sfs: the survivors, counting-sorted by cell sum over S (a
 //     dominator's sum is never larger), go through a sort-filter skyline in
 //     batches of 1,024: each entry is tested against the window of skyline
@@ -23,9 +24,10 @@
 //     last pass tests each skyline and extended entry against the survivors
 //     of its cell-sum bucket with equal cells. Output: [skyline | extended
 //     skyline] ids, each ascending, in the cuboid's slot.
-// A cuboid whose survivors, skyline or extended skyline exceed the
-// shared-memory capacities is flagged; the host then computes it with the
-// single-cuboid pipeline.
+// Cells are those of a grid over the candidates' own quantiles (the caller
+// passes them by point id). A cuboid whose survivors, skyline or extended
+// skyline exceed the capacities is flagged; the host then computes it with
+// the single-cuboid pipeline.
 #include "kernels.cuh"
 
 namespace skc {
