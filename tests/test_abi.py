@@ -70,6 +70,7 @@ def test_null_arguments_are_rejected(built):
     assert L.skc_context_create(0, None) == 1
     assert L.skc_skycube(None, None, None, None) == 1
     assert L.skc_result_info(None, None, None, None) == 1
+    assert L.skc_result_form(None, None, None) == 1
     assert L.skc_autotune(None, None, None, 0, None, None) == 1
     assert L.skc_dataset_signature(None, None, None, None) == 1
     assert L.skc_tuning_count(None, None) == 1
