@@ -224,7 +224,8 @@ def run_serving(sk, ctx, args):
            "queued_p50_ms": round(percentile(queued, 50), 3),
            "queued_p99_ms": round(percentile(queued, 99), 3),
            "run_p50_ms": round(percentile(run, 50), 3), "run_p99_ms": round(percentile(run, 99), 3),
-           "form": "batched (bitmap) form, continuous batching over CUDA-stream slots"}
+           "form": "batched form (per-point bitmaps, or the level form for capped "
+                   "skycubes on many candidates), continuous batching over CUDA-stream slots"}
     nb = min(args.serving_baseline, len(stream))
     if nb:
         def one_at_a_time(mode):
