@@ -199,7 +199,9 @@ int skc_server_submit(skc_server* srv, const float* rows, uint64_t n, int d,
 /* Request on a dataset already resident on the server's context. */
 int skc_server_submit_dataset(skc_server* srv, skc_dataset* ds,
                               const skc_options* opt, uint64_t* ticket);
-/* Blocks until the request is done; hands its result to the caller. */
+/* Blocks until the request is done; hands its result to the caller. Each
+ * ticket has one waiter: a second skc_server_wait on a ticket that is being
+ * waited on, or was already collected, fails with SKC_ERR_INVALID. */
 int skc_server_wait(skc_server* srv, uint64_t ticket, skc_result** out,
                     skc_server_timing* timing);
 int skc_server_stats(skc_server* srv, uint64_t* admitted,

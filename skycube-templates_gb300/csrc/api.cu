@@ -60,6 +60,21 @@ int set_error(int code, const char* fmt, ...) {
 
 void clear_error() { g_err.clear(); }
 
+int check_device_pointer(const void* p, int device, const char* what) {
+  cudaPointerAttributes a{};
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // not sticky: clear it
+    return set_error(SKC_ERR_INVALID, "%s is not a CUDA pointer (%s)", what, cudaGetErrorString(e));
+  }
+  if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+    return set_error(SKC_ERR_INVALID, "%s is not device memory (pointer type %d)", what, (int)a.type);
+  if (a.type == cudaMemoryTypeDevice && a.device != device)
+    return set_error(SKC_ERR_INVALID, "%s lives on device %d, not on the current device %d", what,
+                     a.device, device);
+  return SKC_OK;
+}
+
 static std::atomic<uint64_t> g_launches{0};
 // Launches recorded into a CUDA graph are counted when the graph runs.
 static thread_local bool t_capturing = false;
@@ -1155,6 +1170,10 @@ static int upload_common(skc_context* ctx, const float* rows, uint64_t n, int d,
                          bool from_host, skc_dataset** out) {
   clear_error();
   if (!ctx || !rows || !out) return set_error(SKC_ERR_INVALID, "NULL argument");
+  if (!from_host) {
+    SKC_CUDA(cudaSetDevice(ctx->device));
+    SKC_TRY(check_device_pointer(rows, ctx->device, "d_rows"));
+  }
   return upload_on(ctx, ctx->stream, rows, n, d, from_host, out);
 }
 
@@ -2008,6 +2027,7 @@ struct Request {
   uint64_t footprint = 0;
   std::chrono::steady_clock::time_point t_submit, t_start, t_end;
   bool done = false;
+  bool claimed = false;  // a skc_server_wait has taken this ticket
   int status = SKC_OK;
   std::string err;
   skc_result* result = nullptr;
@@ -2232,8 +2252,14 @@ int skc_server_wait(skc_server* S, uint64_t ticket, skc_result** out, skc_server
     auto it = S->tickets.find(ticket);
     if (it == S->tickets.end()) return set_error(SKC_ERR_INVALID, "unknown ticket %llu", (unsigned long long)ticket);
     q = it->second;
+    // One waiter per ticket: a second one is refused at once instead of
+    // sharing (and later double-freeing) the first one's result.
+    if (q->claimed)
+      return set_error(SKC_ERR_INVALID, "ticket %llu is already being waited on",
+                       (unsigned long long)ticket);
+    q->claimed = true;
     S->cv_done.wait(lk, [&] { return q->done; });
-    S->tickets.erase(it);
+    S->tickets.erase(ticket);  // by key: other waits may have changed the map
   }
   if (t) {
     t->queued_ms = ms_between(q->t_submit, q->t_start);

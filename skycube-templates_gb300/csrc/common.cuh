@@ -20,6 +20,10 @@ namespace skc {
 // message for skc_last_error().
 int set_error(int code, const char* fmt, ...);
 void clear_error();
+// SKC_ERR_INVALID unless p is device (or managed) memory that kernels on
+// `device` can read: host memory passed by mistake fails here, not as an
+// illegal address inside a kernel. Allocates nothing.
+int check_device_pointer(const void* p, int device, const char* what);
 
 #define SKC_TRY(expr)                   \
   do {                                  \

@@ -14,16 +14,17 @@
 // array until the process exits.
 //
 // Host code cannot use the array's name as a device address: on the host the
-// symbol is only a stand-in. The device address is obtained once per device
-// with cudaGetSymbolAddress during the first call made on that device (with
-// that device current) and cached; make that first call before any stream
-// capture. All calls share the one array, which keeps whatever the previous
-// call left in it: the pipeline clears the counters it needs before use, and
-// calls whose work overlaps on the GPU (different streams, or different host
-// threads on one device) race on the array and must be serialised by the
-// caller.
-#include <mutex>
-
+// symbol is only a stand-in. Every call therefore asks the runtime for the
+// array's address in the current device's context (cudaGetSymbolAddress,
+// which allocates nothing) before it launches anything, so a context that
+// was reset or replaced since an earlier call never leaves a stale address.
+// The first call on a device also loads this library's kernels there; make
+// that first call before any stream capture. All calls share the one array,
+// which keeps whatever the previous call left in it: the pipeline clears the
+// counters it needs before use, and calls whose work overlaps on the GPU
+// (different streams, or different host threads on one device) race on the
+// array and must be serialised by the caller. The call is synchronous: it
+// waits on its stream and returns once the statuses are in d_status.
 #include "kernels.cuh"
 
 namespace skc {
@@ -47,22 +48,14 @@ constexpr size_t kNoAllocScratchBytes = kOffSmall + 256;  // minmax[2], n, bad
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch, resolved once per device.
-static std::mutex g_noalloc_mu;
-static void* g_noalloc_addr[64] = {};
-
-static int noalloc_scratch(int device, unsigned char** out) {
-  if (device < 0 || device >= 64) return set_error(SKC_ERR_UNSUPPORTED, "device %d beyond 64", device);
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return set_error(SKC_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed: %s",
-                       cudaGetErrorString(e));
-    g_noalloc_addr[device] = p;
-  }
-  *out = static_cast<unsigned char*>(g_noalloc_addr[device]);
+// Device address of g_noalloc_scratch in the current context.
+static int noalloc_scratch(unsigned char** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return set_error(SKC_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed: %s",
+                     cudaGetErrorString(e));
+  *out = static_cast<unsigned char*>(p);
   return SKC_OK;
 }
 
@@ -91,8 +84,10 @@ extern "C" int skc_skyline_noalloc(const float* d_rows, uint32_t n, int d,
 
   int device = 0;
   SKC_CUDA(cudaGetDevice(&device));
+  SKC_TRY(check_device_pointer(d_rows, device, "d_rows"));
+  SKC_TRY(check_device_pointer(d_status, device, "d_status"));
   unsigned char* base = nullptr;
-  SKC_TRY(noalloc_scratch(device, &base));
+  SKC_TRY(noalloc_scratch(&base));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 
   const uint64_t n_pad = (n + 127) / 128 * 128;

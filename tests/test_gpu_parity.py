@@ -138,3 +138,12 @@ def test_context_destroy_detaches_children():
     assert L.skc_result_cuboid(rh, 1, ctypes.byref(p), ctypes.byref(c)) == 1
     assert L.skc_result_free(rh) == 0
     assert L.skc_dataset_free(dh) == 0
+
+
+def test_device_upload_rejects_host_memory(gpu_ctx):
+    """skc_dataset_upload_device checks that its pointer is device memory:
+    a host buffer passed by mistake is an error, not a kernel fault."""
+    host = np.zeros((8, 3), dtype=np.float32)
+    with pytest.raises(sk.SkycubeError) as e:
+        sk.Dataset(gpu_ctx, device_ptr=host.ctypes.data, n=8, d=3)
+    assert e.value.code == 1 and "device memory" in str(e.value)

@@ -98,3 +98,34 @@ def test_budget_serialises_requests(gpu_ctx):
     assert all(np.array_equal(o, outs[0]) for o in outs)
     assert srv.stats()["peak_in_flight"] == 1
     srv.close()
+
+
+def test_one_waiter_per_ticket(gpu_ctx):
+    """Two threads waiting on the same ticket: one gets the result, the other
+    SKC_ERR_INVALID (never a shared or double-freed result); a wait on a
+    collected ticket is refused too."""
+    import ctypes
+    L = sk.lib()
+    srv = sk.Server(gpu_ctx, slots=1)
+    x = datagen.generate("anticorrelated", 200000, 8, 11)
+    t = srv.submit(x)
+    codes, handles = [None, None], [None, None]
+
+    def wait(i):
+        h = ctypes.c_void_p()
+        codes[i] = L.skc_server_wait(srv.handle, ctypes.c_uint64(t), ctypes.byref(h), None)
+        handles[i] = h
+
+    th = [threading.Thread(target=wait, args=(i,)) for i in (0, 1)]
+    for x_ in th:
+        x_.start()
+    for x_ in th:
+        x_.join()
+    assert sorted(codes) == [0, 1], codes
+    winner = codes.index(0)
+    r = sk.Result(gpu_ctx, handles[winner], 8, 8)
+    assert len(r.cuboid(255)) > 0
+    r.close()
+    h = ctypes.c_void_p()
+    assert L.skc_server_wait(srv.handle, ctypes.c_uint64(t), ctypes.byref(h), None) == 1
+    srv.close()
