@@ -13,14 +13,15 @@ form (MDMC bitmaps, one launch for every cuboid). The JSON line reports:
   roofline   of the dominant kernel (bitmap kernel): algorithmic bytes / its
              event-timed duration against measured HBM bandwidth, plus the
              issue roofline (pair-test lane operations / SM lane-op peak)
-  cpu_baseline  the CPU oracle (restated STSC, all host threads) on a bounded
+  cpu_baseline  the reference's own STSC (all host threads) on a bounded
              sample of the same workload
   reference_sweeps  capped skycubes of 500k x 16 points at the caps of the
              reference's published sweeps, beside its published milliseconds
 
---impl reference times the reference's CPU path (the restated STSC oracle;
-the reference's own build is x86-only) on a bounded sample of the same
-workload with every host thread. Under torchrun each rank computes its own
+--impl reference times the reference's CPU path, its own STSC built from its
+unmodified sources (portable intrinsics on the aarch64 GPU hosts), on a
+bounded sample of the same workload with every host thread, then once on
+the whole workload. Under torchrun each rank computes its own
 replica; N > 1 is replicas only (the path needs no collective).
 """
 import argparse
@@ -54,6 +55,8 @@ def parse_args():
     ap.add_argument("--no-plain", action="store_true", help="skip the per-cuboid form")
     ap.add_argument("--cpu-sample", type=int, default=0, help="points in the CPU sample (0: auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-ref-full", action="store_true",
+                    help="reference arm: skip the one full-size run after the sample steps")
     ap.add_argument("--no-sweeps", action="store_true",
                     help="skip the reference's published sweep workloads")
     ap.add_argument("--serving-queries", type=int, default=600,
@@ -98,21 +101,41 @@ def workload(name, rank):
     return kind, n, d, max_d, seed, x
 
 
-def cpu_sample_run(x, d, max_d, n_sample):
-    """Times the CPU oracle on the first n_sample points of the workload."""
+def cpu_impl():
+    """The CPU implementation timed beside the GPU: the reference's own STSC
+    (oracle/_ref, built from its unmodified sources by build()) when present,
+    else the restated STSC oracle. Returns (run(points, max_d, threads), kind)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
+    if oracle.ref_available():
+        return oracle.ref_stsc, "reference"
+    return oracle.stsc, "port"
+
+
+def cpu_sample_run(x, d, max_d, n_sample):
+    """Times the CPU implementation on the first n_sample points of the
+    workload with every host thread."""
+    run, kind = cpu_impl()
     xs = np.ascontiguousarray(x[:n_sample])
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    oracle.stsc(xs, max_d, threads)
+    run(xs, max_d, threads)
     dt = time.perf_counter() - t0
-    return dt, threads
+    return dt, threads, kind
 
 
 def auto_cpu_sample(name):
     kind = datagen.CONFIGS[name][0]
-    return 80_000 if kind == "anticorrelated" else 300_000
+    return 100_000 if kind == "anticorrelated" else 300_000
+
+
+def cpu_kind_note(kind):
+    if kind == "reference":
+        import platform
+        how = ("its AVX2 dominance tests" if platform.machine() == "x86_64" else
+               "the portable intrinsics of oracle/ref_shim in place of its AVX2 ones")
+        return f"the reference's own STSC (HybridCube<D>, unmodified sources, {how})"
+    return "the restated STSC oracle (the reference's STSC was not built on this host)"
 
 
 # --------------------------------------------------------------------------
@@ -448,12 +471,13 @@ def run_ours(args, world, rank, local):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        ns = args.cpu_sample or auto_cpu_sample(args.workload)
-        dt, threads = cpu_sample_run(x, d, max_d, ns)
-        cpu = {"value": round(ns / dt, 1), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"first {ns:,} points of the same workload, full skycube (all cuboids), "
-                         f"{dt:.2f} s; cost grows faster than linearly in n, so the full 1M "
-                         f"workload runs at a lower rate on the CPU"}
+        ns = min(n, args.cpu_sample or auto_cpu_sample(args.workload))
+        dt, threads, ckind = cpu_sample_run(x, d, max_d, ns)
+        cpu = {"value": round(ns / dt, 1), "unit": UNIT, "cores": threads, "kind": ckind,
+               "sample": f"first {ns:,} points of the same workload, the same cuboids, "
+                         f"{dt:.2f} s, timed around the skycube computation only, with "
+                         f"{cpu_kind_note(ckind)}; its cost grows faster than linearly in n, so "
+                         f"the whole workload runs at a lower rate on the CPU"}
 
     serving = None
     if rank == 0 and world == 1 and args.serving_queries > 0:
@@ -511,32 +535,43 @@ def run_ours(args, world, rank, local):
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the reference's own CPU path for this computation,
+    STSC (HybridCube<D>, the suite's -c oracle) built from its unmodified
+    sources, on every host thread. Each step is a bounded sample of the
+    workload (its first --cpu-sample points, same cuboids); one full-size run
+    follows the timed steps unless --no-ref-full."""
     if rank != 0:
         return
     kind, n, d, max_d, seed, x = workload(args.workload, 0)
-    ns = args.cpu_sample or auto_cpu_sample(args.workload)
-    times, threads = [], os.cpu_count() or 1
+    ns = min(n, args.cpu_sample or auto_cpu_sample(args.workload))
+    times, threads, ckind = [], os.cpu_count() or 1, "port"
     for i in range(args.warmup + args.steps):
-        dt, threads = cpu_sample_run(x, d, max_d, ns)
+        dt, threads, ckind = cpu_sample_run(x, d, max_d, ns)
         if i >= args.warmup:
             times.append(dt)
     mean = sum(times) / len(times)
     value = ns / mean
-    sample = (f"first {ns:,} of the {n:,} points of the workload, full skycube per step; the "
-              f"reference's own STSC build is x86-only (AVX intrinsics), so the restated "
-              f"STSC oracle runs instead")
-    print(json.dumps({
+    sample = (f"first {ns:,} of the {n:,} points of the workload, the same cuboids, per step; "
+              f"{cpu_kind_note(ckind)}, timed around the skycube computation only")
+    out = {
         "impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(mean * 1000, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": f"{kind} n={n:,} d={d} float32, all cuboids", "name": args.workload,
-                   "n": n, "d": d, "max_d": max_d, "seed": seed},
-        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
+        "config": {"workload": f"{kind} n={n:,} d={d} float32, cuboids with <= {max_d} attributes",
+                   "name": args.workload, "n": n, "d": d, "max_d": max_d, "seed": seed},
+        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": ckind,
                          "sample": sample},
         "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-    }), flush=True)
+    }
+    if not args.no_ref_full and ns < n:
+        dt, threads, ckind = cpu_sample_run(x, d, max_d, n)
+        out["full_size"] = {"points": n, "seconds": round(dt, 3), "value": round(n / dt, 1),
+                            "unit": UNIT, "cores": threads, "kind": ckind, "same_config": True,
+                            "note": "one untimed-by-steps run of the whole workload after the "
+                                    "timed sample steps"}
+    print(json.dumps(out), flush=True)
 
 
 def main():

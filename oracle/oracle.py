@@ -5,8 +5,12 @@ check or time the CUDA path; the product never imports it.
 
   stsc(points, max_d, threads)        the C restatement (skycube_oracle.c)
   ref_stsc(points, max_d, threads)    the reference's own STSC built from its
-                                      sources by build_ref.sh (this container
-                                      only; None when not built)
+                                      unmodified sources by build_ref.sh (None
+                                      when not built): with its AVX dominance
+                                      tests on x86-64, with the portable
+                                      intrinsics of ref_shim/ elsewhere;
+                                      shim=True selects the portable build
+                                      made beside the AVX one on x86-64
   bruteforce_bitmaps(points)          definition-level bitmaps for tiny inputs
 
 Both STSC variants return (sky, ext): dicts {cuboid mask: sorted uint32 ids}.
@@ -20,9 +24,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libskycube_ref.so")
+REF_SHIM_LIB = os.path.join(HERE, "_ref", "libskycube_ref_shim.so")
 
 _lib = None
-_ref = None
+_ref = {}
 
 
 def build():
@@ -61,17 +66,27 @@ def lib():
     return _lib
 
 
-def ref_available():
-    return os.path.exists(REF_LIB)
+def ref_available(shim=False):
+    return os.path.exists(REF_SHIM_LIB if shim else REF_LIB)
 
 
-def ref_lib():
-    global _ref
-    if _ref is None:
-        L = ctypes.CDLL(REF_LIB)
+def ref_lib(shim=False):
+    if shim not in _ref:
+        L = ctypes.CDLL(REF_SHIM_LIB if shim else REF_LIB)
         vp, u32, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
-        _ref = _bind(L, "ref_stsc", [vp, u32, i32, i32, i32, i32, i32])
-    return _ref
+        _ref[shim] = _bind(L, "ref_stsc", [vp, u32, i32, i32, i32, i32, i32])
+    return _ref[shim]
+
+
+def build_ref(reference_root=None, shim=False):
+    """Builds the reference's STSC with build_ref.sh; returns True on success."""
+    cmd = ["sh", os.path.join(HERE, "build_ref.sh")]
+    if shim:
+        cmd.append("--shim")
+    if reference_root:
+        cmd.append(reference_root)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    return r.returncode == 0
 
 
 def _collect(fns, h, d, max_d):
@@ -107,13 +122,13 @@ def stsc(points, max_d=0, threads=None):
     return _collect(fns, h, d, md)
 
 
-def ref_stsc(points, max_d=0, threads=None):
-    if not ref_available():
+def ref_stsc(points, max_d=0, threads=None, shim=False):
+    if not ref_available(shim):
         return None
     x = np.ascontiguousarray(points, dtype=np.float32)
     n, d = x.shape
     md = d if max_d <= 0 or max_d > d else max_d
-    fns = ref_lib()
+    fns = ref_lib(shim)
     h = fns[0](x.ctypes.data, n, d, md, _threads(threads), 0, 0)
     if not h:
         raise ValueError(f"reference rejected d={d}")

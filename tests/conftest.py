@@ -17,7 +17,26 @@ def pytest_configure(config):
 
 
 def golden_names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.endswith(".npz") and not f.startswith("digest_"))
+
+
+def load_digest(workload):
+    """The reference STSC's per-cuboid digest of a full-size workload
+    (tests/golden/make_golden.py --digests), or None if not generated."""
+    p = os.path.join(GOLDEN, f"digest_{workload}.npz")
+    return dict(np.load(p)) if os.path.exists(p) else None
+
+
+def id_hash(ids):
+    """64-bit digest of an ascending id list, as make_golden.py computes it."""
+    import hashlib
+    a = np.ascontiguousarray(ids, dtype="<u4")
+    return int.from_bytes(hashlib.blake2b(a.tobytes(), digest_size=8).digest(), "little")
+
+
+def points_hash(x):
+    return id_hash(np.ascontiguousarray(x, dtype="<f4").view("<u4").ravel())
 
 
 def load_golden(name):

@@ -7,9 +7,14 @@ reference's per-cuboid skyline and extended-skyline id sets, so the fixtures
 pin both the C oracle and the CUDA path on machines without the reference.
 
 Usage: python tests/golden/make_golden.py
+       python tests/golden/make_golden.py --digests [workload ...]
+The second form writes digest_<workload>.npz for the full-size benchmark
+workloads (per-cuboid counts and id-list hashes, not the id lists).
 """
+import hashlib
 import os
 import sys
+import time
 
 import numpy as np
 
@@ -76,7 +81,56 @@ def write(name, x, max_d):
     print(f"{name}: n={len(x)} d={d} max_d={max_d} skyline ids={len(si)} extended ids={len(ei)}")
 
 
+def id_hash(ids):
+    """64-bit digest of an ascending id list (BLAKE2b of its little-endian
+    uint32 bytes); the full-size GPU tests compute the same."""
+    a = np.ascontiguousarray(ids, dtype="<u4")
+    return int.from_bytes(hashlib.blake2b(a.tobytes(), digest_size=8).digest(), "little")
+
+
+def points_hash(x):
+    return id_hash(np.ascontiguousarray(x, dtype="<f4").view("<u4").ravel())
+
+
+# Full-size benchmark workloads pinned by digest (datagen.CONFIGS names).
+DIGEST_CASES = ("anticorr-1m-10", "corrq-566k-15-m6", "uniform-100k-6", "ties-581k-10")
+
+
+def write_digest(name, threads):
+    """Per-cuboid digest of the reference's own STSC on one full-size
+    workload: for every computed cuboid its skyline and extended-skyline
+    counts and the 64-bit hashes of both ascending id lists, plus a hash of
+    the generated points (so a generator that differs is reported as such)."""
+    kind, n, d, max_d, seed = datagen.CONFIGS[name]
+    x = datagen.generate(kind, n, d, seed)
+    t0 = time.time()
+    res = oracle.ref_stsc(x, max_d, threads=threads)
+    if res is None:
+        raise SystemExit("reference STSC not built: run oracle/build_ref.sh first")
+    secs = time.time() - t0
+    sky, ext = res
+    cub = np.array(sorted(sky), dtype=np.uint32)
+    out = dict(
+        points_hash=np.uint64(points_hash(x)), n=np.uint64(n), d=np.int32(d),
+        max_d=np.int32(max_d), seed=np.int64(seed), kind=np.array(kind),
+        cuboids=cub,
+        sky_count=np.array([len(sky[c]) for c in cub], dtype=np.uint64),
+        ext_count=np.array([len(ext[c]) for c in cub], dtype=np.uint64),
+        sky_hash=np.array([id_hash(sky[c]) for c in cub], dtype=np.uint64),
+        ext_hash=np.array([id_hash(ext[c]) for c in cub], dtype=np.uint64),
+        reference_seconds=np.float64(secs), reference_threads=np.int32(threads))
+    np.savez_compressed(os.path.join(HERE, f"digest_{name}.npz"), **out)
+    print(f"digest {name}: {len(cub)} cuboids, {int(out['sky_count'].sum())} skyline ids, "
+          f"{int(out['ext_count'].sum())} extended ids; reference STSC {secs:.1f} s on "
+          f"{threads} threads", flush=True)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "--digests":
+        names = sys.argv[2:] or DIGEST_CASES
+        for name in names:
+            write_digest(name, os.cpu_count() or 1)
+        return
     for name, (kind, n, d, max_d, seed) in CASES.items():
         write(name, datagen.generate(kind, n, d, seed), max_d)
     for name, (x, d) in edge_cases().items():

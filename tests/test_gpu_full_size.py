@@ -1,5 +1,11 @@
 """Full-size parity on the benchmark workloads.
 
+Every full-size workload is pinned against the reference's own STSC through
+a per-cuboid digest (counts and 64-bit hashes of the ascending skyline and
+extended-skyline id lists, tests/golden/digest_*.npz, made by
+tests/golden/make_golden.py --digests), for the batched form the benchmark
+times, the batched form with extended skylines, and the per-cuboid form.
+
 The two execution forms are independent GPU algorithms (per-point bitmaps in
 one launch; per-cuboid median-partition skylines), so their exact agreement
 on every cuboid of the full-size workloads is checked for all of them; the
@@ -12,6 +18,7 @@ import pytest
 
 import oracle
 import skycube_gb300 as sk
+from conftest import id_hash, load_digest, points_hash
 from skycube_gb300 import datagen
 
 pytestmark = pytest.mark.gpu
@@ -65,3 +72,35 @@ def test_full_space_always_present_under_cap(gpu_ctx):
         r = sk.skycube(gpu_ctx, ds, algo, mode, max_d=2)
         assert np.array_equal(r.cuboid(511), sky[511])
         assert len(r.cuboid(0b111)) == 0
+
+
+DIGESTS = ["uniform-100k-6", "anticorr-1m-10", "ties-581k-10", "corrq-566k-15-m6"]
+
+
+@pytest.mark.parametrize("form", ["mdmc/batched", "sdsc/batched", "sdsc/plain"])
+@pytest.mark.parametrize("name", DIGESTS)
+def test_full_size_digest(gpu_ctx, name, form):
+    dg = load_digest(name)
+    if dg is None:
+        pytest.skip(f"no reference digest for {name}")
+    kind, n, d, m, seed = datagen.CONFIGS[name]
+    x = datagen.generate(kind, n, d, seed)
+    assert points_hash(x) == int(dg["points_hash"]), "the generator gives other points than the digest's"
+    algo, mode = form.split("/")
+    ext = algo == "sdsc"
+    ds = sk.Dataset(gpu_ctx, x)
+    r = sk.skycube(gpu_ctx, ds, algo, mode, max_d=m, want_extended=ext)
+    r.download()
+    bad = []
+    for i, c in enumerate(dg["cuboids"].tolist()):
+        s_ = r.cuboid(c)
+        if len(s_) != int(dg["sky_count"][i]) or id_hash(s_) != int(dg["sky_hash"][i]):
+            bad.append(("skyline", c, len(s_), int(dg["sky_count"][i])))
+        if ext:
+            e_ = r.extended(c)
+            if len(e_) != int(dg["ext_count"][i]) or id_hash(e_) != int(dg["ext_hash"][i]):
+                bad.append(("extended", c, len(e_), int(dg["ext_count"][i])))
+    assert not bad, f"{len(bad)} cuboids differ from the reference, first: {bad[:5]}"
+    assert r.info()["total_skyline_ids"] == int(dg["sky_count"].sum())
+    r.close()
+    ds.close()

@@ -82,3 +82,26 @@ def test_prefilter_keeps_full_space_statuses(kind, seed, K):
     fsky, fext = oracle.stsc(x[keep])
     assert np.array_equal(keep[fsky[full]], sky[full])
     assert np.array_equal(keep[fext[full]], ext[full])
+
+
+@pytest.mark.skipif(not (oracle.ref_available() and oracle.ref_available(shim=True)),
+                    reason="the AVX and portable builds of the reference STSC are not both built here")
+@pytest.mark.parametrize("case", golden_names() + ["gen:ties:7000:10:4", "gen:anticorrelated:5000:8:8",
+                                                   "gen:correlated_q:3000:15:5", "gen:uniform:2500:16:3"])
+def test_reference_portable_build_matches_avx_build(case):
+    """The reference STSC built with the portable intrinsics of
+    oracle/ref_shim (as on the aarch64 GPU hosts) gives the same skyline and
+    extended skyline of every cuboid as its AVX2 build, on every golden input
+    and on larger seeded ones (ties, d = 15 and 16 included)."""
+    if case.startswith("gen:"):
+        _, kind, n, d, max_d = case.split(":")
+        x = datagen.generate(kind, int(n), int(d), 77)
+        max_d = int(max_d)
+    else:
+        x, max_d, _, _ = load_golden(case)
+    a = oracle.ref_stsc(x, max_d)
+    b = oracle.ref_stsc(x, max_d, shim=True)
+    assert a[0].keys() == b[0].keys()
+    for c in a[0]:
+        assert np.array_equal(a[0][c], b[0][c]), f"skyline of cuboid {c}"
+        assert np.array_equal(a[1][c], b[1][c]), f"extended skyline of cuboid {c}"
