@@ -59,12 +59,20 @@ def parse_args():
                     help="reference arm: skip the one full-size run after the sample steps")
     ap.add_argument("--no-sweeps", action="store_true",
                     help="skip the reference's published sweep workloads")
-    ap.add_argument("--serving-queries", type=int, default=600,
+    ap.add_argument("--serving-queries", type=int, default=2000,
                     help="queries of the serving stream (0: skip serving)")
-    ap.add_argument("--serving-rate", type=float, default=40.0, help="Poisson arrival rate, queries/s")
+    ap.add_argument("--serving-rate", type=float, default=20.0, help="Poisson arrival rate, queries/s")
     ap.add_argument("--serving-slots", type=int, default=4)
-    ap.add_argument("--serving-baseline", type=int, default=60,
+    ap.add_argument("--serving-baseline", type=int, default=200,
                     help="queries served one at a time with the plain form for comparison")
+    ap.add_argument("--record-counters", metavar="NCU_CSV",
+                    help="write profiles/kernel_counters_<workload>.json from the --csv output of "
+                         "ncu --print-units base --metrics smsp__inst_executed.sum,"
+                         "dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum "
+                         "-k regex:k_bitmaps over this benchmark, with the sha256 of the bitmap "
+                         "kernel's sources, then exit")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other benchmark configurations (100k x 6, ties, 15-d capped)")
     return ap.parse_args()
 
 
@@ -195,6 +203,39 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
+def bitmap_sources_sha():
+    """sha256 of the bitmap kernel's sources (mdmc.cu and the headers it
+    includes): a recorded instruction count is valid only for these."""
+    import hashlib
+    h = hashlib.sha256()
+    csrc = os.path.join(REPO, "skycube-templates_gb300", "csrc")
+    for f in ("mdmc.cu", "common.cuh", "kernels.cuh"):
+        with open(os.path.join(csrc, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()
+
+
+def kernel_counts(workload):
+    """Counters of the bitmap kernel from profiles/kernel_counters_<workload>.json
+    (an ncu capture of the full-size workload): warp instructions and DRAM
+    bytes per launch, used only when the capture's recorded source hash
+    matches the sources built now."""
+    path = os.path.join(REPO, "profiles", f"kernel_counters_{workload}.json")
+    if not os.path.exists(path):
+        return {"provenance": {"file": None, "matches": False}}
+    with open(path) as f:
+        t = json.load(f).get("k_bitmaps", {})
+    sha = bitmap_sources_sha()
+    ok = t.get("sources_sha256") == sha
+    prov = {"file": os.path.relpath(path, REPO), "matches": ok,
+            "sources_sha256": sha[:16], "recorded_sha256": (t.get("sources_sha256") or "")[:16]}
+    if not ok:
+        return {"provenance": prov}
+    return {"warp_inst_per_launch": t.get("warp_inst_per_launch"),
+            "dram_bytes_per_launch": t.get("dram_bytes_per_launch"),
+            "useful": t.get("useful"), "provenance": prov}
+
+
 def flush_l2(buf):
     buf.zero_()
 
@@ -209,16 +250,21 @@ def percentile(v, p):
 
 
 def run_serving(sk, ctx, args):
-    """Serving stream: queries arrive Poisson at --serving-rate, each over its
-    own seeded dataset (n log-uniform in [1e3, 1e6], d in 4..16, uniform /
-    correlated / anticorrelated); half capped skycubes (<= 4 attributes), half
-    skylines of one random subspace. Served by the continuous-batching server
-    (host rows in, host results out). The first --serving-baseline queries
-    are also served one at a time with the plain per-cuboid form on the same
-    arrival times (sequential queue on a virtual clock from measured service
-    times)."""
+    """Serving stream (config 5): --serving-queries queries arrive Poisson at
+    --serving-rate, each over its own seeded dataset (n log-uniform in
+    [1e3, 1e6], d in 4..16, uniform / correlated / anticorrelated; a seeded
+    window of a per-(distribution, d) pool, datagen.ServingPools); half
+    skycubes (every cuboid for d <= 10, else a cap of 2..6 attributes drawn
+    per query), half skylines of one random subspace. Served by the
+    continuous-batching server (host rows in, host results out). The first
+    --serving-baseline queries are also served one at a time with the plain
+    per-cuboid form and with the batched form, on the same arrival times
+    (a sequential queue on a virtual clock from measured service times)."""
     stream = datagen.serving_stream(count=args.serving_queries, rate_qps=args.serving_rate, seed=7)
-    data = [datagen.generate(q["kind"], q["n"], q["d"], q["seed"]) for q in stream]
+    pools = datagen.ServingPools()
+    t_gen = time.perf_counter()
+    data = [pools.dataset(q) for q in stream]
+    gen_s = time.perf_counter() - t_gen
     srv = sk.Server(ctx, slots=args.serving_slots)
     for x, q in list(zip(data, stream))[:8]:  # warm-up (kernels, pools)
         r, _ = srv.wait(srv.submit(x, max_d=q["max_d"], subspace=q["subspace"]))
@@ -230,16 +276,22 @@ def run_serving(sk, ctx, args):
         if delay > 0:
             time.sleep(delay)
         tickets.append(srv.submit(x, max_d=q["max_d"], subspace=q["subspace"]))
-    lat, queued, run = [], [], []
+    lat, queued, run, dev = [], [], [], []
     for t in tickets:
         r, tm = srv.wait(t)
         lat.append(tm["total_ms"])
         queued.append(tm["queued_ms"])
         run.append(tm["run_ms"])
+        dev.append(tm["device_ms"])
         r.close()
     span = max(time.perf_counter() - t0, stream[-1]["arrival_s"])
     stats = srv.stats()
     srv.close()
+    sky = [i for i, q in enumerate(stream) if not q["subspace"]]
+
+    def pct(idx, p):
+        return round(percentile([lat[i] for i in idx], p), 3) if idx else None
+
     out = {"queries": len(stream), "rate_qps": args.serving_rate, "slots": args.serving_slots,
            "p50_ms": round(percentile(lat, 50), 3), "p99_ms": round(percentile(lat, 99), 3),
            "mean_ms": round(sum(lat) / len(lat), 3), "max_ms": round(max(lat), 3),
@@ -247,6 +299,12 @@ def run_serving(sk, ctx, args):
            "queued_p50_ms": round(percentile(queued, 50), 3),
            "queued_p99_ms": round(percentile(queued, 99), 3),
            "run_p50_ms": round(percentile(run, 50), 3), "run_p99_ms": round(percentile(run, 99), 3),
+           "device_p50_ms": round(percentile(dev, 50), 3),
+           "device_p99_ms": round(percentile(dev, 99), 3),
+           "skycube_queries": len(sky), "skycube_p50_ms": pct(sky, 50), "skycube_p99_ms": pct(sky, 99),
+           "skyline_p50_ms": pct([i for i in range(len(stream)) if stream[i]["subspace"]], 50),
+           "skyline_p99_ms": pct([i for i in range(len(stream)) if stream[i]["subspace"]], 99),
+           "datasets_host_s": round(gen_s, 2),
            "form": "batched form (per-point bitmaps, or the level form for capped "
                    "skycubes on many candidates), continuous batching over CUDA-stream slots"}
     nb = min(args.serving_baseline, len(stream))
@@ -329,6 +387,129 @@ def run_reference_sweeps(sk, ctx):
             "note": "reference_ms: the authors' SDSC runs on one GPU of their own machine "
                     "(not a GB300) over their data files; these inputs are seeded synthetic "
                     "stand-ins with the same shape and distribution family"}
+
+
+def run_configs(sk, ctx, flush):
+    """The other benchmark configurations (the headline is 1M x 10
+    anticorrelated): 100k x 6 uniform in the plain per-cuboid form and
+    batched; 581k x 10 ties batched with the work parameters autotuned over
+    grid depths 2..4; 566k x 15 correlated (quantised), cuboids of <= 6
+    attributes, as a CUDA-graph plan. Device ms: CUDA events around the
+    computation, L2 flushed before each run, median of 5 after a warm-up.
+    e2e ms: host rows in (pinned), every cuboid's ids in host memory."""
+    import torch
+
+    def dev_ms(fn, reps=5):
+        fn().close()
+        ms = []
+        for _ in range(reps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            r = fn()
+            ms.append(ctx.last_device_ms())
+            r.close()
+        return round(statistics.median(ms), 3)
+
+    def e2e_ms(x, reps=3, **opts):
+        xp = torch.from_numpy(x).pin_memory().numpy()
+        best = None
+        for _ in range(reps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ds = sk.Dataset(ctx, xp)
+            r = sk.skycube(ctx, ds, **opts)
+            r.download()
+            t = (time.perf_counter() - t0) * 1000.0
+            r.close()
+            ds.close()
+            best = t if best is None else min(best, t)
+        return round(best, 3)
+
+    out = {}
+    # 100k x 6 uniform: the plain form (one launch sequence per cuboid)
+    kind, n, d, m, seed = datagen.CONFIGS["uniform-100k-6"]
+    x = datagen.generate(kind, n, d, seed)
+    ds = sk.Dataset(ctx, x)
+    plain = dev_ms(lambda: sk.skycube(ctx, ds, "sdsc", "plain", max_d=m))
+    batched = dev_ms(lambda: sk.skycube(ctx, ds, "mdmc", "batched", max_d=m))
+    r = sk.skycube(ctx, ds, "sdsc", "plain", max_d=m)
+    ids = r.info()["total_skyline_ids"]
+    r.close()
+    ds.close()
+    out["uniform-100k-6"] = {
+        "workload": f"uniform n={n:,} d={d}, all {2 ** d - 1} cuboids", "plain_ms": plain,
+        "plain_points_per_s": round(n / (plain / 1000.0), 1), "batched_ms": batched,
+        "batched_over_plain": round(plain / batched, 2),
+        "plain_e2e_ms": e2e_ms(x, algo="sdsc", mode="plain", max_d=m),
+        "batched_e2e_ms": e2e_ms(x, algo="mdmc", mode="batched", max_d=m),
+        "total_skyline_ids": ids}
+
+    # 581k x 10 ties: batched, work parameters autotuned over depths 2..4
+    kind, n, d, m, seed = datagen.CONFIGS["ties-581k-10"]
+    x = datagen.generate(kind, n, d, seed)
+    ds = sk.Dataset(ctx, x)
+    ctx.tuning_clear()
+    default = dev_ms(lambda: sk.skycube(ctx, ds, "mdmc", "batched", max_d=m))
+    tuned = []
+    for depth in (2, 3, 4):
+        params, ms = sk.autotune(ctx, ds, repeats=2, algo="mdmc", mode="batched", depth=depth)
+        tuned.append((ms, depth, params))
+    tuned.sort(key=lambda t: t[0])
+    _, depth, params = tuned[0]
+    opts = {k: params[k] for k in ("depth", "pq_size", "tile_points", "chunk", "blocks_per_sm")}
+    batched = dev_ms(lambda: sk.skycube(ctx, ds, "mdmc", "batched", max_d=m, **opts))
+    flush_l2(flush)
+    torch.cuda.synchronize()
+    r = sk.skycube(ctx, ds, "sdsc", "plain", max_d=m)
+    plain = round(ctx.last_device_ms(), 3)
+    ids = r.info()["total_skyline_ids"]
+    r.close()
+    ctx.tuning_clear()
+    ds.close()
+    out["ties-581k-10"] = {
+        "workload": f"ties n={n:,} d={d} (integer-valued), all {2 ** d - 1} cuboids",
+        "batched_ms": batched, "points_per_s": round(n / (batched / 1000.0), 1),
+        "autotuned": {"over_depths": [2, 3, 4], "chosen": opts,
+                      "tuning_ms_by_depth": {str(t[1]): round(t[0], 3) for t in tuned}},
+        "default_params_ms": default, "plain_ms": plain,
+        "batched_over_plain": round(plain / batched, 1),
+        "batched_e2e_ms": e2e_ms(x, algo="mdmc", mode="batched", max_d=m, **opts),
+        "total_skyline_ids": ids}
+
+    # 566k x 15 correlated (quantised), -m 6: the batched form as a CUDA graph
+    kind, n, d, m, seed = datagen.CONFIGS["corrq-566k-15-m6"]
+    x = datagen.generate(kind, n, d, seed)
+    ds = sk.Dataset(ctx, x)
+    plan = sk.Plan(ctx, ds, algo="mdmc", mode="batched", max_d=m)
+    graph = dev_ms(plan.execute)
+    batched = dev_ms(lambda: sk.skycube(ctx, ds, "mdmc", "batched", max_d=m))
+    xp = torch.from_numpy(x).pin_memory().numpy()
+    g_e2e = None
+    for _ in range(3):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ds.update(xp)
+        r = plan.execute()
+        r.download()
+        t = (time.perf_counter() - t0) * 1000.0
+        ids = r.info()["total_skyline_ids"]
+        r.close()
+        g_e2e = t if g_e2e is None else min(g_e2e, t)
+    pinfo = plan.info()
+    plan.close()
+    ds.close()
+    ncub = sum(1 for c in range(1, 1 << d) if bin(c).count("1") <= m) + 1
+    out["corrq-566k-15-m6"] = {
+        "workload": f"correlated (quantised to 0.1/{d}) n={n:,} d={d}, {ncub:,} cuboids of <= {m} "
+                    f"attributes plus the full space, capped bitmaps",
+        "graph_ms": graph, "points_per_s": round(n / (graph / 1000.0), 1), "batched_ms": batched,
+        "graph_e2e_ms": round(g_e2e, 3), "kernels_per_replay": pinfo["kernels"],
+        "total_skyline_ids": ids,
+        "plain_ms_note": "the per-cuboid form takes about 31 s here (9,949 cuboids, one launch "
+                         "sequence and host round trip each); not re-run by the benchmark"}
+    return out
 
 
 def run_ours(args, world, rank, local):
@@ -455,19 +636,29 @@ def run_ours(args, world, rank, local):
     alg_bytes = m * (d * 4 + 16) + m * words * 4
     achieved_gbs = alg_bytes / (kern / 1000.0) / 1e9
     hbm = float(peaks.get("hbm_gbs", 6800.0))
-    pairs = float(m) * float(m)
     sm_mhz = clk.get("sm_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
     issue_peak = 152 * 4 * sm_mhz * 1e6  # warp instructions/s: 152 SMs x 4 schedulers
-    # Counters of the same kernel from one ncu capture of this workload
-    # (profiles/kernel_counters_<workload>.json): DRAM bytes and warp
-    # instructions per launch.
-    traffic, inst = None, None
-    tpath = os.path.join(REPO, "profiles", f"kernel_counters_{args.workload}.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            t = json.load(f).get("k_bitmaps", {})
-        traffic = t.get("dram_bytes_per_launch")
-        inst = t.get("warp_inst_per_launch")
+    counts = kernel_counts(args.workload)
+    inst = counts.get("warp_inst_per_launch")
+    roofline = {
+        "kernel": "k_bitmaps", "bound": "issue",
+        "achieved": round(inst / (kern / 1000.0) / 1e9, 2) if inst else None,
+        "peak": round(issue_peak / 1e9, 2), "unit": "G warp-instructions/s",
+        "frac": round(inst / (kern / 1000.0) / issue_peak, 4) if inst else None,
+        "traffic": counts.get("dram_bytes_per_launch"),
+        "kernel_ms": round(kern, 3), "warp_inst_per_launch": inst,
+        "counts": counts.get("provenance"),
+        "peak_source": f"152 SMs x 4 schedulers x median SM clock under load ({sm_mhz:.0f} MHz)",
+        "note": "the bitmap kernel is bound by instruction issue (integer ALU), not DRAM: "
+                "warp instructions per launch from an ncu capture of this workload whose "
+                "kernel sources match the ones built (sha256 recorded with the count; "
+                "null when they differ), divided by the live event-timed kernel duration",
+        "hbm": {"achieved": round(achieved_gbs, 3), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved_gbs / hbm, 6), "alg_bytes": alg_bytes,
+                "peak_source": peak_kind},
+    }
+    if counts.get("useful"):
+        roofline["useful_work"] = counts["useful"]
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -479,6 +670,9 @@ def run_ours(args, world, rank, local):
                          f"{cpu_kind_note(ckind)}; its cost grows faster than linearly in n, so "
                          f"the whole workload runs at a lower rate on the CPU"}
 
+    configs = None
+    if rank == 0 and world == 1 and not args.no_configs:
+        configs = run_configs(sk, ctx, flush)
     serving = None
     if rank == 0 and world == 1 and args.serving_queries > 0:
         serving = run_serving(sk, ctx, args)
@@ -500,21 +694,7 @@ def run_ours(args, world, rank, local):
         "e2e": {"value": round(world * n / e2e_mean, 1), "unit": UNIT,
                 "h2d_bytes_per_step": n * d * 4, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(e2e_mean * 1000, 3)},
-        "roofline": {"kernel": "k_bitmaps", "bound": "hbm", "achieved": round(achieved_gbs, 3),
-                     "peak": hbm, "unit": "GB/s", "frac": round(achieved_gbs / hbm, 6),
-                     "traffic": traffic, "peak_source": peak_kind,
-                     "kernel_ms": round(kern, 3), "alg_bytes": alg_bytes},
-        "issue_roofline": {
-            "kernel": "k_bitmaps",
-            "achieved": round(inst / (kern / 1000.0) / 1e9, 2) if inst else None,
-            "peak": round(issue_peak / 1e9, 2), "unit": "G warp-instructions/s",
-            "frac": round(inst / (kern / 1000.0) / issue_peak, 4) if inst else None,
-            "warp_inst_per_launch": inst,
-            "pair_space": int(pairs),
-            "note": "the kernel is bound by instruction issue, not DRAM: warp instructions "
-                    "per launch from one ncu capture of this workload, divided by the live "
-                    "event-timed kernel duration; peak = 152 SMs x 4 schedulers x median SM "
-                    "clock under load"},
+        "roofline": roofline,
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": int(launches),
@@ -525,6 +705,8 @@ def run_ours(args, world, rank, local):
     out["graph"] = graph
     if plain:
         out["plain"] = plain
+    if configs:
+        out["configs"] = configs
     if serving:
         out["serving"] = serving
     if sweeps:
@@ -574,8 +756,43 @@ def run_reference(args, world, rank):
     print(json.dumps(out), flush=True)
 
 
+def record_counters(csv_path, workload):
+    """Per-launch counters of the bitmap kernel from an ncu --csv log (the
+    last k_bitmaps launch in it) into profiles/kernel_counters_<workload>.json."""
+    import csv
+    rows = []
+    with open(csv_path) as f:
+        lines = [ln for ln in f if ln.startswith('"')]
+    for r in csv.DictReader(lines):
+        if "k_bitmaps" in r.get("Kernel Name", ""):
+            rows.append(r)
+    if not rows:
+        raise SystemExit(f"no k_bitmaps launch in {csv_path}")
+    last = max(int(r["ID"]) for r in rows)
+    vals = {}
+    for r in rows:
+        if int(r["ID"]) == last:
+            vals[r["Metric Name"]] = float(r["Metric Value"].replace(",", ""))
+    out = {"k_bitmaps": {
+        "warp_inst_per_launch": int(vals["smsp__inst_executed.sum"]),
+        "dram_bytes_per_launch": int(vals["dram__bytes_read.sum"] + vals["dram__bytes_write.sum"]),
+        "dram_bytes_read": int(vals["dram__bytes_read.sum"]),
+        "dram_bytes_write": int(vals["dram__bytes_write.sum"]),
+        "gpu_time_ms_under_ncu": round(vals["gpu__time_duration.sum"] / 1e6, 3),
+        "kernel_name": next(r["Kernel Name"] for r in rows if int(r["ID"]) == last),
+        "sources_sha256": bitmap_sources_sha(),
+        "source": os.path.basename(csv_path)}}
+    path = os.path.join(REPO, "profiles", f"kernel_counters_{workload}.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+    print(json.dumps(out))
+
+
 def main():
     args = parse_args()
+    if args.record_counters:
+        record_counters(args.record_counters, args.workload)
+        return
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)

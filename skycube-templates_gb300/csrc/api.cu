@@ -250,6 +250,7 @@ struct RunParams {
   int chunk = 1;          // bitmap kernel: candidates per queue grab
   int blocks_per_sm = 0;  // bitmap kernel: 0 = occupancy limit
 };
+constexpr int kDefaultChunk = 1;
 
 // Device-side result of the full-space step.
 struct FullSpace {
@@ -992,7 +993,7 @@ static int resolve_params(skc_dataset* ds, cudaStream_t s, const skc_options& o,
   else if (o.pq_size == 0) pq = have ? tv.pq_size : (n >= kPrefilterMinPoints ? kDefaultPruners : 0);
   P.pq_size = (pq > 0 && n > 2ull * (uint64_t)pq) ? pq : 0;
   P.tile_points = o.tile_points ? o.tile_points : have ? tv.tile_points : kDefaultTilePoints;
-  P.chunk = o.chunk ? o.chunk : have ? tv.chunk : 1;
+  P.chunk = o.chunk ? o.chunk : have ? tv.chunk : kDefaultChunk;
   P.blocks_per_sm = o.blocks_per_sm ? o.blocks_per_sm : have ? tv.blocks_per_sm : 0;
   *out = P;
   return SKC_OK;
@@ -1755,7 +1756,7 @@ int skc_autotune(skc_context* ctx, skc_dataset* ds, const skc_options* base, int
                                   : (n >= kPrefilterMinPoints ? kDefaultPruners : 0);
   cur.pq_size = (pq0 > 0 && n > 2ull * (uint64_t)pq0) ? pq0 : 0;
   cur.tile_points = o.tile_points ? o.tile_points : kDefaultTilePoints;
-  cur.chunk = o.chunk ? o.chunk : 1;
+  cur.chunk = o.chunk ? o.chunk : kDefaultChunk;
   cur.blocks_per_sm = o.blocks_per_sm;
 
   auto time_run = [&](const RunParams& P, float* ms) -> int {
@@ -1789,7 +1790,7 @@ int skc_autotune(skc_context* ctx, skc_dataset* ds, const skc_options* base, int
     }
     return SKC_OK;
   };
-  if (!o.depth) SKC_TRY(try_values(&RunParams::depth, {7, 6, 5, 4, 3}));
+  if (!o.depth) SKC_TRY(try_values(&RunParams::depth, {7, 6, 5, 4, 3, 2}));
   if (!o.pq_size) {
     std::vector<int> pqs;
     for (int v : {0, 32, 128, 512, kMaxPruners})

@@ -318,8 +318,12 @@ __device__ void nr_close_smem(uint32_t* sat_s, int lane, int cap) {
   __syncwarp();
 }
 
+// Register budgets: d <= 10 (STRICT in registers) 8 CTAs per SM uncapped
+// (32 registers, no spill), 6 capped; d >= 11, 4 CTAs (64 registers).
+// Unbounded, the allocator took 48 registers at d = 10 (40 warps per SM
+// instead of 64) and up to 136 at d = 16.
 template <int D, bool CAP>
-__global__ void __launch_bounds__(256) k_bitmaps(
+__global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
     const uint4* __restrict__ pcells, const float* __restrict__ px,
     uint64_t p_pad, const uint4* __restrict__ qcells,
     const float* __restrict__ qx, const uint4* __restrict__ bmin,
@@ -361,20 +365,17 @@ __global__ void __launch_bounds__(256) k_bitmaps(
     const uint32_t p1 = min(pend, p0 + chunk);
     for (uint32_t p = p0; p < p1; ++p) {
     const uint4 pc4 = pcells[p];
-    uint32_t pc[NW], pH[NW];
+    uint32_t pH[NW];  // p's cells with the guard bits set (cells are < 128)
 #pragma unroll
-    for (int w = 0; w < NW; ++w) {
-      pc[w] = word_of(pc4, w);
-      pH[w] = pc[w] | kGuard;
-    }
+    for (int w = 0; w < NW; ++w) pH[w] = word_of(pc4, w) | kGuard;
     // p's median mask over the partitioning attributes 0 .. B-1
     uint32_t pmask = 0;
 #pragma unroll
     for (int k = 0; k < D; ++k)
       if (k < B) pmask |= ((word_of(pc4, k >> 2) >> (8 * (k & 3) + sh)) & 1u) << k;
-    float pv[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) pv[k] = px[(uint64_t)k * p_pad + p];
+    // p's floats are read where a cell ties (rare; cached), not held in
+    // registers.
+    const float* pxp = px + p;
 
     // STRICT starts with the empty subspace so that q's worse on every
     // attribute (U == 0) test as "nothing new".
@@ -414,6 +415,113 @@ __global__ void __launch_bounds__(256) k_bitmaps(
       return (word >> (S & 31)) & 1u;
     };
 
+    // Tests the q's of one block (position qi in lane t) against p and
+    // applies their strict and tie sets.
+    auto test_q = [&](uint32_t qi) {
+      const uint4 q4 = qcells[qi];
+      uint32_t U = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w)
+        U |= pack_guards(ge_bytes(pH[w], word_of(q4, w))) << (4 * w);
+      U &= NSUB - 1;
+      const bool hit = in_strict(U);
+      if (__all_sync(kFull, hit)) return;
+
+      uint32_t le = 0, lt = 0;
+      if (!hit) {
+        uint32_t G = 0;  // cell(q) >= cell(p)
+#pragma unroll
+        for (int w = 0; w < NW; ++w)
+          G |= pack_guards(ge_bytes(word_of(q4, w) | kGuard, pH[w] ^ kGuard)) << (4 * w);
+        G &= NSUB - 1;
+        const uint32_t Y = U & ~G;  // certainly q < p
+        const uint32_t Z = U & G;   // equal cells: compare the floats
+        le = Y;
+        lt = Y;
+        if (Z) {
+#pragma unroll
+          for (int k = 0; k < D; ++k) {
+            if (Z & (1u << k)) {
+              const float a = qx[(uint64_t)k * p_pad + qi];
+              const float b = pxp[(uint64_t)k * p_pad];
+              if (a <= b) le |= 1u << k;
+              if (a < b) lt |= 1u << k;
+            }
+          }
+        }
+      }
+      const bool t_lt = in_strict(lt);
+      const bool t_le = in_strict(le);
+      // Tie pairs go to the tie map (one atomic per lane); a tie set
+      // inside STRICT changes nothing.
+      const bool tie_lane = !hit && le != lt && !t_le;
+      const uint32_t tb = __ballot_sync(kFull, tie_lane);
+      if (tb) {
+        if constexpr (BS::A_SMEM) {
+          if (!touched) {
+            for (uint32_t w = lane; w < AW; w += 32) A[w] = 0;
+            __syncwarp();
+            touched = true;
+          }
+          if (tie_lane) atomicOr(&A[le >> 1], lt << (16 * (le & 1)));
+        } else {
+          uint32_t* tlist = wsm + W + BS::CHUNK_WORDS;
+          const uint32_t nt = __popc(tb);
+          if (tmode != 2 && tcount + nt <= BS::LIST_WORDS) {
+            if (tie_lane) tlist[tcount + __popc(tb & ((1u << lane) - 1u))] = le | (lt << 16);
+            tcount += nt;
+            tmode = 1;
+            __syncwarp();
+          } else {
+            if (tmode != 2) {
+              // Too many pairs: move to the global map (zeroed, then
+              // the listed pairs OR-ed in).
+              for (uint32_t w = lane; w < AW; w += 32) A[w] = 0;
+              __syncwarp();
+              if ((uint32_t)lane < tcount) {
+                const uint32_t e = tlist[lane];
+                atomicOr(&A[(e & 0xffffu) >> 1], (e >> 16) << (16 * (e & 1u)));
+              }
+              tmode = 2;
+            }
+            if (tie_lane) atomicOr(&A[le >> 1], lt << (16 * (le & 1)));
+          }
+        }
+      }
+      // Strict updates: down(LT) into STRICT, one pair at a time.
+      uint32_t todo = __ballot_sync(kFull, !hit && !t_lt);
+      while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const uint32_t L = __shfl_sync(kFull, lt, src);
+        if (in_strict(L)) continue;  // covered by an earlier update
+        if constexpr (CAP) dirty = true;
+        if (REG) {
+          if ((wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
+        } else {
+          // Only the words under L: the subsets of L >> 5. Lane j
+          // takes the j-th subset of the lowest five bits of L >> 5
+          // and walks all subsets of the remaining bits.
+          const uint32_t sl = c_submask[L & 31];
+          uint32_t base, rest;
+          if (split_words(L >> 5, lane, &base, &rest)) {
+            uint32_t sub = 0;
+            do {
+              sat_s[base | sub] |= sl;
+              sub = (sub - rest) & rest;
+            } while (sub);
+          }
+          __syncwarp();
+        }
+      }
+      if constexpr (CAP && REG) {
+        if (dirty) {
+          sat = nr_close_reg<D>(sat, wi, cap);
+          dirty = false;
+        }
+      }
+    };
+
     uint32_t next_blk = 0;  // blocks below this one were already visited
     // Partitions are tested 32 at a time (lane t tests partition b0 + t):
     // a partition is skipped when the attributes its points may win on
@@ -433,150 +541,64 @@ __global__ void __launch_bounds__(256) k_bitmaps(
       }
       // in_strict shuffles across the warp: every lane must evaluate it.
       const bool sb_strict = in_strict(Sb);
-      const bool part_skip = (qbeg_l == qend_l) || sb_strict;
-      uint32_t parts = __ballot_sync(kFull, !part_skip);
-      while (parts) {
-        const int ps = __ffs(parts) - 1;
-        parts &= parts - 1;
-        if constexpr (CAP) {  // the set may have grown since the ballot
-          if (in_strict(__shfl_sync(kFull, Sb, ps))) continue;
+      const bool sel = (qbeg_l != qend_l) && !sb_strict;
+      const uint32_t parts = __ballot_sync(kFull, sel);
+      if (!parts) continue;
+      // The blocks of all selected partitions form one list, so their box
+      // tests fill the 32 lanes: lane t's partition owns blocks [bf, be).
+      // A block shared with the previous selected partition (or visited
+      // under an earlier ballot) is visited once; its q's from a skipped
+      // partition are tested too (any q's update is valid).
+      const uint32_t be = (qend_l + 31) / 32;
+      const uint32_t lower = parts & ((1u << lane) - 1u);
+      const int prev = lower ? 31 - __clz(lower) : 0;
+      const uint32_t prev_be = __shfl_sync(kFull, be, prev);
+      const uint32_t bf = max(qbeg_l / 32, lower ? prev_be : next_blk);
+      const uint32_t cnt = (sel && be > bf) ? be - bf : 0u;
+      uint32_t incl = cnt;  // inclusive prefix sum of the block counts
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const uint32_t total = __shfl_sync(kFull, incl, 31);
+      next_blk = max(next_blk, __shfl_sync(kFull, be, 31 - __clz(parts)));
+      // list entry g of lane t's partition is block g + base (mod 2^32)
+      const uint32_t base = bf - (incl - cnt);
+      for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+        maybe_close();
+        const uint32_t g = t0 + lane;
+        // owner of list entry g: the first lane whose inclusive sum is > g
+        int j = 0;
+#pragma unroll
+        for (int step = 16; step; step >>= 1) {
+          const uint32_t v = __shfl_sync(kFull, incl, j + step - 1);
+          if (v <= g) j += step;
         }
-        const uint32_t qbeg = __shfl_sync(kFull, qbeg_l, ps);
-        const uint32_t qend = __shfl_sync(kFull, qend_l, ps);
-        // A block shared with the previous partition is visited once; its
-        // q's from a skipped partition are tested too (any q's update is
-        // valid).
-        const uint32_t blk_end = (qend + 31) / 32;
-        const uint32_t blk_first = max(qbeg / 32, next_blk);
-        next_blk = max(next_blk, blk_end);
-        // Blocks are tested 32 at a time against their byte-wise minimum
-        // cells, then the surviving blocks are walked one by one.
-        for (uint32_t k0 = blk_first; k0 < blk_end; k0 += 32) {
-          maybe_close();
-          const uint32_t kb = k0 + lane;
-          uint32_t Ub = 0;
-          if (kb < blk_end) {
-            const uint4 bm = bmin[kb];
+        const uint32_t kb = g + __shfl_sync(kFull, base, j);
+        const bool in_list = g < total;
+        // Blocks are tested against their byte-wise minimum cells, then
+        // the surviving blocks are walked one by one.
+        uint32_t Ub = 0;
+        if (in_list) {
+          const uint4 bm = bmin[kb];
 #pragma unroll
-            for (int w = 0; w < NW; ++w)
-              Ub |= pack_guards(ge_bytes(pH[w], word_of(bm, w))) << (4 * w);
-            Ub &= NSUB - 1;
+          for (int w = 0; w < NW; ++w)
+            Ub |= pack_guards(ge_bytes(pH[w], word_of(bm, w))) << (4 * w);
+          Ub &= NSUB - 1;
+        }
+        const bool ub_strict = in_strict(Ub);  // every lane (shuffle)
+        uint32_t blocks = __ballot_sync(kFull, in_list && !ub_strict);
+        if constexpr (CAP && !REG) since += 1 + __popc(blocks);
+        while (blocks) {
+          const int bs = __ffs(blocks) - 1;
+          blocks &= blocks - 1;
+          if constexpr (CAP && REG) {  // closed after every update
+            if (in_strict(__shfl_sync(kFull, Ub, bs))) continue;
           }
-          const bool ub_strict = in_strict(Ub);  // every lane (shuffle)
-          const bool blk_skip = (kb >= blk_end) || ub_strict;
-          uint32_t blocks = __ballot_sync(kFull, !blk_skip);
-          if constexpr (CAP && !REG) since += 1 + __popc(blocks);
-          while (blocks) {
-            const int bs = __ffs(blocks) - 1;
-            blocks &= blocks - 1;
-            if constexpr (CAP && REG) {  // closed after every update
-              if (in_strict(__shfl_sync(kFull, Ub, bs))) continue;
-            }
-            // The q arrays are padded to whole blocks with entries that add
-            // nothing (k_pad_q), so every lane of a block can be tested.
-            const uint32_t qi = (k0 + bs) * 32 + lane;
-            const uint4 q4 = qcells[qi];
-            uint32_t U = 0;
-#pragma unroll
-            for (int w = 0; w < NW; ++w)
-              U |= pack_guards(ge_bytes(pH[w], word_of(q4, w))) << (4 * w);
-            U &= NSUB - 1;
-            const bool hit = in_strict(U);
-            if (__all_sync(kFull, hit)) continue;
-
-            uint32_t le = 0, lt = 0;
-            if (!hit) {
-              uint32_t G = 0;  // cell(q) >= cell(p)
-#pragma unroll
-              for (int w = 0; w < NW; ++w)
-                G |= pack_guards(ge_bytes(word_of(q4, w) | kGuard, pc[w])) << (4 * w);
-              G &= NSUB - 1;
-              const uint32_t Y = U & ~G;  // certainly q < p
-              const uint32_t Z = U & G;   // equal cells: compare the floats
-              le = Y;
-              lt = Y;
-              if (Z) {
-#pragma unroll
-                for (int k = 0; k < D; ++k) {
-                  if (Z & (1u << k)) {
-                    const float a = qx[(uint64_t)k * p_pad + qi];
-                    if (a <= pv[k]) le |= 1u << k;
-                    if (a < pv[k]) lt |= 1u << k;
-                  }
-                }
-              }
-            }
-            const bool t_lt = in_strict(lt);
-            const bool t_le = in_strict(le);
-            // Tie pairs go to the tie map (one atomic per lane); a tie set
-            // inside STRICT changes nothing.
-            const bool tie_lane = !hit && le != lt && !t_le;
-            const uint32_t tb = __ballot_sync(kFull, tie_lane);
-            if (tb) {
-              if constexpr (BS::A_SMEM) {
-                if (!touched) {
-                  for (uint32_t w = lane; w < AW; w += 32) A[w] = 0;
-                  __syncwarp();
-                  touched = true;
-                }
-                if (tie_lane) atomicOr(&A[le >> 1], lt << (16 * (le & 1)));
-              } else {
-                uint32_t* tlist = wsm + W + BS::CHUNK_WORDS;
-                const uint32_t nt = __popc(tb);
-                if (tmode != 2 && tcount + nt <= BS::LIST_WORDS) {
-                  if (tie_lane) tlist[tcount + __popc(tb & ((1u << lane) - 1u))] = le | (lt << 16);
-                  tcount += nt;
-                  tmode = 1;
-                  __syncwarp();
-                } else {
-                  if (tmode != 2) {
-                    // Too many pairs: move to the global map (zeroed, then
-                    // the listed pairs OR-ed in).
-                    for (uint32_t w = lane; w < AW; w += 32) A[w] = 0;
-                    __syncwarp();
-                    if ((uint32_t)lane < tcount) {
-                      const uint32_t e = tlist[lane];
-                      atomicOr(&A[(e & 0xffffu) >> 1], (e >> 16) << (16 * (e & 1u)));
-                    }
-                    tmode = 2;
-                  }
-                  if (tie_lane) atomicOr(&A[le >> 1], lt << (16 * (le & 1)));
-                }
-              }
-            }
-            // Strict updates: down(LT) into STRICT, one pair at a time.
-            uint32_t todo = __ballot_sync(kFull, !hit && !t_lt);
-            while (todo) {
-              const int src = __ffs(todo) - 1;
-              todo &= todo - 1;
-              const uint32_t L = __shfl_sync(kFull, lt, src);
-              if (in_strict(L)) continue;  // covered by an earlier update
-              if constexpr (CAP) dirty = true;
-              if (REG) {
-                if ((wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
-              } else {
-                // Only the words under L: the subsets of L >> 5. Lane j
-                // takes the j-th subset of the lowest five bits of L >> 5
-                // and walks all subsets of the remaining bits.
-                const uint32_t sl = c_submask[L & 31];
-                uint32_t base, rest;
-                if (split_words(L >> 5, lane, &base, &rest)) {
-                  uint32_t sub = 0;
-                  do {
-                    sat_s[base | sub] |= sl;
-                    sub = (sub - rest) & rest;
-                  } while (sub);
-                }
-                __syncwarp();
-              }
-            }
-            if constexpr (CAP && REG) {
-              if (dirty) {
-                sat = nr_close_reg<D>(sat, wi, cap);
-                dirty = false;
-              }
-            }
-          }
+          // The q arrays are padded to whole blocks with entries that add
+          // nothing (k_pad_q), so every lane of a block can be tested.
+          test_q(__shfl_sync(kFull, kb, bs) * 32 + lane);
         }
       }
     }

@@ -79,16 +79,19 @@ CONFIGS = {
 
 
 def serving_stream(count=2000, rate_qps=20.0, seed=7, n_min=1_000, n_max=1_000_000,
-                   skycube_max_d=4):
+                   full_skycube_max_dims=10, cap_range=(2, 6)):
     """Queries of the serving workload, in arrival order.
 
     Each query has its own seeded dataset: n log-uniform in [n_min, n_max],
     d uniform in {4..16}, distribution uniform over uniform (independent),
-    correlated and anticorrelated. Half are skycube queries (every cuboid of
-    at most `skycube_max_d` attributes), half skyline queries on one random
-    subspace of at least two attributes. Arrivals are Poisson with the given
-    rate (exponential gaps). Returns a list of dicts with keys arrival_s,
-    kind, n, d, seed, max_d, subspace.
+    correlated and anticorrelated. Half are skycube queries, half skyline
+    queries on one random subspace of at least two attributes. A skycube
+    query computes every cuboid when d <= full_skycube_max_dims, else every
+    cuboid of at most max_d attributes with max_d drawn uniformly from
+    cap_range (a whole 16-d skycube of a million points has tens of
+    billions of ids). Arrivals are Poisson with the given rate
+    (exponential gaps). Returns a list of dicts with keys arrival_s, kind,
+    n, d, seed, max_d, subspace.
     """
     rng = np.random.default_rng(seed)
     out = []
@@ -100,7 +103,8 @@ def serving_stream(count=2000, rate_qps=20.0, seed=7, n_min=1_000, n_max=1_000_0
         d = int(rng.integers(4, 17))
         kind = kinds[int(rng.integers(0, 3))]
         if rng.random() < 0.5:
-            q = {"max_d": min(d, skycube_max_d), "subspace": 0}
+            cap = int(rng.integers(cap_range[0], cap_range[1] + 1))
+            q = {"max_d": d if d <= full_skycube_max_dims else cap, "subspace": 0}
         else:
             while True:
                 sub = int(rng.integers(1, 1 << d))
@@ -109,3 +113,29 @@ def serving_stream(count=2000, rate_qps=20.0, seed=7, n_min=1_000, n_max=1_000_0
             q = {"max_d": 0, "subspace": sub}
         out.append({"arrival_s": t, "kind": kind, "n": n, "d": d, "seed": 10_000 + i, **q})
     return out
+
+
+class ServingPools:
+    """Datasets of the serving stream, drawn without generating each one
+    whole: for every (distribution, d) one pool of `pool_n` seeded points is
+    generated once, and a query's dataset is the window of n consecutive
+    pool rows at an offset drawn from the query's own seed. Points of a pool
+    are independent draws of the distribution, so every window is a sample
+    of it of size n. dataset(q) returns a read-only view (no copy)."""
+
+    def __init__(self, pool_n=1_000_000, seed=4242):
+        self.pool_n = pool_n
+        self.seed = seed
+        self.pools = {}
+
+    def pool(self, kind, d):
+        key = (kind, d)
+        if key not in self.pools:
+            self.pools[key] = generate(kind, self.pool_n, d, self.seed + 97 * d + KINDS.index(kind))
+        return self.pools[key]
+
+    def dataset(self, q):
+        p = self.pool(q["kind"], q["d"])
+        n = min(q["n"], self.pool_n)
+        off = int(np.random.default_rng(q["seed"]).integers(0, self.pool_n - n + 1))
+        return p[off:off + n]

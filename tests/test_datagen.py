@@ -36,3 +36,31 @@ def test_correlated_q_quantised():
 def test_unknown_kind():
     with pytest.raises(ValueError):
         datagen.generate("nope", 10, 3)
+
+
+def test_serving_stream_shape():
+    qs = datagen.serving_stream(count=400, rate_qps=20.0, seed=7)
+    assert len(qs) == 400
+    t = [q["arrival_s"] for q in qs]
+    assert all(b > a for a, b in zip(t, t[1:]))
+    assert 10 < t[-1] < 40  # Poisson at 20/s
+    for q in qs:
+        assert 1000 <= q["n"] <= 1_000_000 and 4 <= q["d"] <= 16
+        if q["subspace"]:
+            assert q["max_d"] == 0 and bin(q["subspace"]).count("1") >= 2
+            assert q["subspace"] < (1 << q["d"])
+        elif q["d"] <= 10:
+            assert q["max_d"] == q["d"]
+        else:
+            assert 2 <= q["max_d"] <= 6
+    caps = {q["max_d"] for q in qs if not q["subspace"] and q["d"] > 10}
+    assert caps == {2, 3, 4, 5, 6}
+
+
+def test_serving_pools_windows():
+    pools = datagen.ServingPools(pool_n=50_000)
+    q = {"kind": "anticorrelated", "d": 6, "n": 1234, "seed": 10_001}
+    a, b = pools.dataset(q), pools.dataset(q)
+    assert a.shape == (1234, 6) and a.flags.c_contiguous and np.array_equal(a, b)
+    other = pools.dataset({**q, "seed": 10_002})
+    assert not np.array_equal(a, other)
