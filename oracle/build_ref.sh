@@ -15,7 +15,8 @@
 #       the include path. On x86-64, --shim writes
 #       oracle/_ref/libskycube_ref_shim.so instead, so the two builds can be
 #       compared (tests/test_oracle.py).
-#   oracle/build_ref.sh --stage REFERENCE_ROOT
+#   oracle/build_ref.sh --stage [REFERENCE_ROOT]
+#       (default $SKC_REFERENCE_ROOT, else /root/reference)
 #       Copies the thirteen reference files this build reads into
 #       oracle/_ref/src (git-ignored), so a host without the checkout can
 #       build them. Nothing outside oracle/_ref is written.
@@ -28,7 +29,7 @@ src/utilities/SubTuple.h src/utilities/common2.h src/utilities/dt_avx2.h
 src/utilities/pq_filter.h src/utilities/lattice_utilities.h src/utilities/lattice_utilities.cpp"
 
 if [ "$1" = "--stage" ]; then
-  REF=$2
+  REF=${2:-${SKC_REFERENCE_ROOT:-/root/reference}}
   [ -f "$REF/src/stsc/HybridCube.cpp" ] || { echo "reference sources not found at $REF" >&2; exit 2; }
   for f in $FILES; do
     mkdir -p "$OUT/src/$(dirname "$f")"

@@ -190,6 +190,111 @@ struct Arena {
 
 static inline uint64_t round_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
 
+// ---------------------------------------------------------------------------
+// Host <-> device copies of the pipelines go through pinned staging memory
+// owned by the calling host thread (two halves, used in turn, each guarded
+// by an event). A copy from or to pageable memory otherwise goes through
+// the driver's staging path, and one request's pageable read-back queued
+// behind its long kernel held up the pageable copies of every other request
+// on the device (serving: 5 ms requests took 500 ms behind a 575 ms one).
+// Pinned user memory is copied directly. The staging memory lives until the
+// thread exits.
+constexpr size_t kStageHalf = 8u << 20;
+struct HostStaging {
+  unsigned char* buf = nullptr;  // 2 * kStageHalf pinned bytes
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  bool used[2] = {false, false};
+  int next = 0;
+  ~HostStaging() {
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+    if (buf) cudaFreeHost(buf);
+  }
+};
+static thread_local HostStaging t_stage;
+
+static int staging(HostStaging** out) {
+  HostStaging& S = t_stage;
+  if (!S.buf) {
+    SKC_CUDA(cudaHostAlloc((void**)&S.buf, 2 * kStageHalf, cudaHostAllocPortable));
+    for (auto& e : S.ev) SKC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  *out = &S;
+  return SKC_OK;
+}
+
+static bool is_pinned(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// Host -> device on stream s; `src` may be reused once this returns.
+static int copy_h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (!bytes) return SKC_OK;
+  if (is_pinned(src)) {
+    SKC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    return SKC_OK;
+  }
+  HostStaging* S;
+  SKC_TRY(staging(&S));
+  for (size_t o = 0; o < bytes; o += kStageHalf) {
+    const size_t c = std::min(kStageHalf, bytes - o);
+    const int h = S->next;
+    S->next ^= 1;
+    if (S->used[h]) SKC_CUDA(cudaEventSynchronize(S->ev[h]));
+    unsigned char* b = S->buf + h * kStageHalf;
+    memcpy(b, static_cast<const unsigned char*>(src) + o, c);
+    SKC_CUDA(cudaMemcpyAsync(static_cast<unsigned char*>(dst) + o, b, c, cudaMemcpyHostToDevice, s));
+    SKC_CUDA(cudaEventRecord(S->ev[h], s));
+    S->used[h] = true;
+  }
+  return SKC_OK;
+}
+
+// Device -> host on stream s; returns once `dst` holds the data (after the
+// work queued before it on s).
+static int copy_d2h(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (!bytes) return SKC_OK;
+  if (is_pinned(dst)) {
+    SKC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+    SKC_CUDA(cudaStreamSynchronize(s));
+    return SKC_OK;
+  }
+  HostStaging* S;
+  SKC_TRY(staging(&S));
+  // chunk k goes to half (k & 1); chunk k - 1 is copied out while k moves
+  size_t prev_o = 0, prev_c = 0;
+  int prev_h = -1;
+  for (size_t o = 0;; o += kStageHalf) {
+    const bool more = o < bytes;
+    int h = -1;
+    size_t c = 0;
+    if (more) {
+      c = std::min(kStageHalf, bytes - o);
+      h = S->next;
+      S->next ^= 1;
+      if (S->used[h]) SKC_CUDA(cudaEventSynchronize(S->ev[h]));
+      SKC_CUDA(cudaMemcpyAsync(S->buf + h * kStageHalf, static_cast<const unsigned char*>(src) + o, c,
+                               cudaMemcpyDeviceToHost, s));
+      SKC_CUDA(cudaEventRecord(S->ev[h], s));
+      S->used[h] = true;
+    }
+    if (prev_h >= 0) {
+      SKC_CUDA(cudaEventSynchronize(S->ev[prev_h]));
+      memcpy(static_cast<unsigned char*>(dst) + prev_o, S->buf + prev_h * kStageHalf, prev_c);
+    }
+    if (!more) break;
+    prev_o = o;
+    prev_c = c;
+    prev_h = h;
+  }
+  return SKC_OK;
+}
+
 // Partition tables over B-bit masks, built once per context (partition.cu):
 // one device buffer [rank | unrank | sub_off | sub_list].
 static int level_tables(skc_context* ctx, int B, LevelTables* out) {
@@ -356,8 +461,7 @@ static int run_full_space(Exec& E, skc_dataset* ds, const RunParams& P, Arena& A
     F.h_counts[2] = (uint32_t)cap;
     return SKC_OK;
   }
-  SKC_CUDA(cudaMemcpyAsync(F.h_counts, F.counts, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  SKC_CUDA(cudaStreamSynchronize(s));
+  SKC_TRY(copy_d2h(F.h_counts, F.counts, 3 * sizeof(uint32_t), s));
   T.mark("full: compaction");
   return SKC_OK;
 }
@@ -478,8 +582,9 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
     // One launch per batch of points with a host round trip after each
     // (bitmaps of the batch copied to pinned host memory).
     const uint32_t batch = d >= 16 ? 2300 : 5600;
-    uint32_t* h_stage = nullptr;
-    SKC_CUDA(cudaMallocHost(&h_stage, (size_t)batch * W * sizeof(uint32_t)));
+    // (host memory: the thread's staging, chunk by chunk; a pinned block
+    // allocated and freed per call would wait for the whole device on free)
+    std::vector<uint32_t> h_stage((size_t)batch * W);
     int st = SKC_OK;
     for (uint64_t p0 = 0; p0 < m && st == SKC_OK; p0 += batch) {
       const uint32_t p1 = (uint32_t)std::min<uint64_t>(m, p0 + batch);
@@ -488,12 +593,8 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
       ba.p_end = p1;
       st = launch_bitmaps(s, d, ctx->num_sms, ba);
       if (st != SKC_OK) break;
-      cudaError_t e = cudaMemcpyAsync(h_stage, dom + p0 * W, (size_t)(p1 - p0) * W * sizeof(uint32_t),
-                                      cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-      if (e != cudaSuccess) st = set_error(SKC_ERR_CUDA, "batch copy failed: %s", cudaGetErrorString(e));
+      st = copy_d2h(h_stage.data(), dom + p0 * W, (size_t)(p1 - p0) * W * sizeof(uint32_t), s);
     }
-    cudaFreeHost(h_stage);
     SKC_TRY(st);
   }
   T.mark("bitmap kernel");
@@ -525,8 +626,7 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
       total = E.plan->ids_cap[pass];
       SKC_TRY(launch_stat_u64(s, csr + nsub, E.plan->stats, 1 + pass));
     } else {
-      SKC_CUDA(cudaMemcpyAsync(&total, csr + nsub, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-      SKC_CUDA(cudaStreamSynchronize(s));
+      SKC_TRY(copy_d2h(&total, csr + nsub, sizeof(uint64_t), s));
     }
     uint32_t* ids;
     SKC_TRY(A.alloc(&ids, total));
@@ -562,10 +662,10 @@ struct CuboidScratch {
   PartScratch ps;
   uint32_t *cand = nullptr, *d_m = nullptr, *blk0 = nullptr, *blk1 = nullptr, *cnt = nullptr;
   uint8_t* status = nullptr;
-  uint32_t* h_cnt = nullptr;  // pinned [2]
-  ~CuboidScratch() {
-    if (h_cnt) cudaFreeHost(h_cnt);
-  }
+  // Counts read back per cuboid. Pageable on purpose: freeing pinned host
+  // memory (cudaFreeHost) waits for the whole device, which stalled a
+  // serving request for as long as another request's kernels ran.
+  uint32_t h_cnt[2] = {0, 0};
 };
 
 static int cuboid_scratch(Arena& A, int d, uint64_t mmax, CuboidScratch* cs) {
@@ -592,7 +692,6 @@ static int cuboid_scratch(Arena& A, int d, uint64_t mmax, CuboidScratch* cs) {
   SKC_TRY(A.alloc(&cs->blk0, nblk));
   SKC_TRY(A.alloc(&cs->blk1, nblk));
   SKC_TRY(A.alloc(&cs->cnt, 2));
-  SKC_CUDA(cudaMallocHost(&cs->h_cnt, 2 * sizeof(uint32_t)));
   return SKC_OK;
 }
 
@@ -612,9 +711,7 @@ static int cuboid_lists(Exec& E, skc_dataset* ds, FullSpace& F, int depth, Arena
   SKC_TRY(A.alloc(oext, mc));
   SKC_TRY(launch_status_compact(s, cs.status, cand, cs.d_m, mc, 0, cs.blk0, cs.blk1, *osky,
                                 *oext, cs.cnt, cs.cnt + 1));
-  cudaError_t e = cudaMemcpyAsync(cs.h_cnt, cs.cnt, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return set_error(SKC_ERR_CUDA, "cuboid %u: %s", c, cudaGetErrorString(e));
+  SKC_TRY(copy_d2h(cs.h_cnt, cs.cnt, 2 * sizeof(uint32_t), s));
   *nsky = cs.h_cnt[0];
   *next = cs.h_cnt[1];
   return SKC_OK;
@@ -646,8 +743,8 @@ static int assemble_csr(Exec& E, Arena& A, int d, int max_d, bool want_ext,
     std::vector<const uint32_t*> srcs(nsub, nullptr);
     for (uint32_t c = 0; c < nsub; ++c)
       if (off[c + 1] > off[c]) srcs[c] = srcv[c];
-    SKC_CUDA(cudaMemcpyAsync(d_off, off.data(), (nsub + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-    SKC_CUDA(cudaMemcpyAsync(d_srcs, srcs.data(), nsub * sizeof(void*), cudaMemcpyHostToDevice, s));
+    SKC_TRY(copy_h2d(d_off, off.data(), (nsub + 1) * sizeof(uint64_t), s));
+    SKC_TRY(copy_h2d(d_srcs, srcs.data(), nsub * sizeof(void*), s));
     SKC_TRY(launch_csr_gather(s, d_srcs, d_off, nsub, ids));
     SKC_CUDA(cudaStreamSynchronize(s));  // host vectors above must outlive the copies
     A.release(d_off);
@@ -721,141 +818,260 @@ static int run_sdsc_plain(Exec& E, skc_dataset* ds, int max_d,
   return assemble_csr(E, A, d, max_d, true, sky, nsky, ext, next, R);
 }
 
-// Capped skycubes (max_d <= kLvMaxDims) by lattice level (levels.cu): every
-// cuboid of a level in one filter launch and one sort-filter launch per
-// group of cuboids, each from its smallest computed parent's skyline +
-// extended skyline or the full space's candidates. Cuboids over the
-// kernel's capacities go through the single-cuboid pipeline.
-constexpr uint64_t kLvScratchBytes = 2048ull << 20;  // survivor scratch per group
+// Capped skycubes (max_d <= kLvMaxDims) in the lattice form (levels.cu):
+// every wanted cuboid of every job in ONE persistent launch whose device
+// work queue runs the lattice levels top down, each cuboid from its
+// smallest computed parent's skyline + extended skyline (or the full
+// space's candidates). Cuboids over the kernel's capacities are computed
+// afterwards with the single-cuboid pipeline.
+constexpr uint64_t kLvScratchBytes = 2048ull << 20;  // survivor scratch per launch
 constexpr uint32_t kLvMaxSurvivors = 262144;         // per cuboid
-// More cuboids over the capacities than this on the first level (heavy
+// More cuboids over the capacities than this on a job's first level (heavy
 // exact ties: the per-cuboid fallback would dominate) and the bitmap form
-// takes over; run_levels then returns kLvGiveUp with the result untouched.
+// takes over; the job's status is then kLvGiveUp with its result untouched.
 constexpr int kLvMaxFallbacks = 16;
 constexpr int kLvGiveUp = 1000;
 
-static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d, int depth,
-                      Arena& A, FullSpace& F, skc_result* R, Tracer& T) {
-  cudaStream_t s = E.stream;
-  const int d = ds->d;
-  const uint32_t nsub = 1u << d, full = nsub - 1;
-  std::vector<uint32_t*> sky(nsub, nullptr), ext(nsub, nullptr);
-  std::vector<uint64_t> nsky(nsub, 0), next(nsub, 0);
-  std::vector<const uint32_t*> lst(nsub, nullptr);  // sky + ext of a computed cuboid
-  std::vector<char> done(nsub, 0);
-  sky[full] = F.sky;
-  ext[full] = F.ext;
-  nsky[full] = F.h_counts[0];
-  next[full] = F.h_counts[1];
-  lst[full] = F.cand;
-  done[full] = 1;
-  CuboidScratch cs;
-  bool cs_ready = false;
-  int fallbacks = 0;
-  // Cells on a grid of the candidates' own quantiles, by point id: on the
-  // full-space grid most candidates of correlated data share one cell on
-  // every attribute, which leaves the cell sums no order to give.
-  const uint64_t m = F.h_counts[2];
-  float* pivots;
-  uint4 *cc, *lv_cells;
-  SKC_TRY(A.alloc(&pivots, (uint64_t)kMaxDims * kMaxPivots));
-  SKC_TRY(A.alloc(&cc, m));
-  SKC_TRY(A.alloc(&lv_cells, ds->n));
-  SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, F.cand, F.counts + 2, m, depth, pivots, cc));
-  SKC_TRY(launch_scatter_u4(s, cc, F.cand, F.counts + 2, m, lv_cells));
+struct LatticeJob {
+  skc_dataset* ds = nullptr;
+  int max_d = 0;
+  int depth = kMaxDepth;
+  bool want_ext = false;
+  FullSpace* F = nullptr;
+  skc_result* R = nullptr;
+  int status = SKC_OK;  // per job: SKC_OK or kLvGiveUp
+  // filled by run_lattice
+  uint4* lv_cells = nullptr;
+  uint32_t* d_index = nullptr;
+  uint32_t cub0 = 0;
+  std::vector<uint32_t> masks;
+};
 
-  for (int lev = max_d; lev >= 1; --lev) {
+static int run_lattice(Exec& E, std::vector<LatticeJob>& jobs, Arena& A, Tracer& T) {
+  skc_context* ctx = E.ctx;
+  cudaStream_t s = E.stream;
+  const uint32_t nj = (uint32_t)jobs.size();
+  // 1. Per job: cells on a grid of the candidates' own quantiles, by point id
+  // (on the full-space grid most candidates of correlated data share one
+  // cell on every attribute, which leaves the cell sums no order to give),
+  // and its cuboid table (levels top down, masks ascending).
+  std::vector<LtJob> hjobs(nj);
+  std::vector<uint32_t> c_mask, c_job;
+  std::vector<int> c_level;
+  std::vector<std::vector<uint32_t>> index(nj);
+  uint64_t max_cand = 1;
+  int top = 0;
+  for (uint32_t j = 0; j < nj; ++j) {
+    LatticeJob& J = jobs[j];
+    skc_dataset* ds = J.ds;
+    const int d = ds->d;
+    const uint64_t m = J.F->h_counts[2];
+    float* pivots;
+    uint4* cc;
+    SKC_TRY(A.alloc(&pivots, (uint64_t)kMaxDims * kMaxPivots));
+    SKC_TRY(A.alloc(&cc, std::max<uint64_t>(1, m)));
+    SKC_TRY(A.alloc(&J.lv_cells, ds->n));
+    SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, J.F->cand, J.F->counts + 2, m, J.depth,
+                                pivots, cc));
+    SKC_TRY(launch_scatter_u4(s, cc, J.F->cand, J.F->counts + 2, m, J.lv_cells));
+    J.cub0 = (uint32_t)c_mask.size();
+    const uint32_t full = (1u << d) - 1;
+    index[j].assign(1u << d, 0xffffffffu);
+    for (int lev = J.max_d; lev >= 1; --lev)
+      for (uint32_t c = 1; c < full; ++c)
+        if (__builtin_popcount(c) == lev) {
+          index[j][c] = (uint32_t)c_mask.size();
+          c_mask.push_back(c);
+          c_job.push_back(j);
+          c_level.push_back(lev);
+        }
+    J.masks.assign(c_mask.begin() + J.cub0, c_mask.end());
+    SKC_TRY(A.alloc(&J.d_index, 1u << d));
+    SKC_TRY(copy_h2d(J.d_index, index[j].data(), sizeof(uint32_t) << d, s));
+    hjobs[j] = LtJob{ds->x, ds->n_pad, J.lv_cells, J.F->cand, (uint32_t)m, J.d_index, d, J.max_d};
+    max_cand = std::max<uint64_t>(max_cand, m);
+    top = std::max(top, J.max_d);
+  }
+  const uint32_t ncub = (uint32_t)c_mask.size();
+
+  // 2. Work queue: per level (top down) groups of cuboids that fit the
+  // survivor scratch, each as phases P, F and S.
+  int grid = 0;
+  SKC_TRY(lattice_grid(ctx->num_sms, &grid));
+  const uint32_t cap = (uint32_t)std::min<uint64_t>(max_cand, kLvMaxSurvivors);
+  const uint32_t G = (uint32_t)std::max<uint64_t>(1, kLvScratchBytes / ((uint64_t)cap * 10));
+  std::vector<uint32_t> c_scr(ncub, 0), it_cub, it_arg, it_phase, ph_size;
+  std::vector<uint8_t> ph_kind;
+  uint32_t g_used = 1;
+  for (int lev = top; lev >= 1; --lev) {
     std::vector<uint32_t> cubs;
-    for (uint32_t c = 1; c < full; ++c)
-      if (__builtin_popcount(c) == lev) cubs.push_back(c);
-    const uint32_t nc = (uint32_t)cubs.size();
-    std::vector<uint32_t> src(nc), hn(nc);
-    std::vector<const uint32_t*> hl(nc);
-    uint64_t maxn = 0;
-    for (uint32_t i = 0; i < nc; ++i) {
-      src[i] = min_parent(cubs[i], d, nsky, next, done);
-      hl[i] = lst[src[i]];
-      hn[i] = (uint32_t)(nsky[src[i]] + next[src[i]]);
-      maxn = std::max<uint64_t>(maxn, hn[i]);
+    for (uint32_t c = 0; c < ncub; ++c)
+      if (c_level[c] == lev) cubs.push_back(c);
+    for (size_t g0 = 0; g0 < cubs.size(); g0 += G) {
+      const uint32_t ng = (uint32_t)std::min<size_t>(G, cubs.size() - g0);
+      g_used = std::max(g_used, ng);
+      for (int kind = 0; kind < 3; ++kind) {
+        const uint32_t ph = (uint32_t)ph_size.size();
+        uint32_t count = 0;
+        for (uint32_t i = 0; i < ng; ++i) {
+          const uint32_t c = cubs[g0 + i];
+          c_scr[c] = i;
+          uint32_t nsl = 1;
+          if (kind == 1) {
+            // a job's first level filters its full candidate list; lower
+            // levels their parent's slot (at most kLvSlot entries)
+            const bool first = c_level[c] == jobs[c_job[c]].max_d;
+            const uint64_t len = first ? jobs[c_job[c]].F->h_counts[2] : kLvSlot;
+            const uint64_t chunks = std::max<uint64_t>(1, (len + kLvChunk - 1) / kLvChunk);
+            nsl = (uint32_t)std::min<uint64_t>(
+                std::min<uint64_t>(chunks, 0xffffu), std::max<uint64_t>(1, (2ull * grid + ng - 1) / ng));
+          }
+          for (uint32_t sl = 0; sl < nsl; ++sl) {
+            it_cub.push_back(c);
+            it_arg.push_back(sl | (nsl << 16));
+            it_phase.push_back(ph);
+            ++count;
+          }
+        }
+        ph_size.push_back(count);
+        ph_kind.push_back((uint8_t)kind);
+      }
     }
-    const uint32_t cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(maxn, kLvMaxSurvivors));
-    const uint32_t G = (uint32_t)std::max<uint64_t>(
-        1, std::min<uint64_t>(nc, kLvScratchBytes / ((uint64_t)cap * 10)));
-    uint32_t *d_masks, *d_n, *slot, *outs, *cnt, *surv_id, *srt;
-    const uint32_t** d_lists;
-    uint16_t* surv_key;
-    SKC_TRY(A.alloc(&d_masks, nc));
-    SKC_TRY(A.alloc(&d_n, nc));
-    SKC_TRY(A.alloc(&d_lists, nc));
-    SKC_TRY(A.alloc(&slot, (uint64_t)nc * kLvSlot));
-    SKC_TRY(A.alloc(&outs, 3ull * nc));
-    SKC_TRY(A.alloc(&cnt, G));
-    SKC_TRY(A.alloc(&surv_id, (uint64_t)G * cap));
-    SKC_TRY(A.alloc(&surv_key, (uint64_t)G * cap));
-    SKC_TRY(A.alloc(&srt, (uint64_t)G * cap));
-    uint32_t *pr_c, *pr_n;
-    float* pr_v;
-    SKC_TRY(A.alloc(&pr_c, (uint64_t)G * kLvPruners));
-    SKC_TRY(A.alloc(&pr_v, (uint64_t)G * kLvMaxDims * kLvPruners));
-    SKC_TRY(A.alloc(&pr_n, G));
-    SKC_CUDA(cudaMemcpyAsync(d_masks, cubs.data(), nc * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    SKC_CUDA(cudaMemcpyAsync(d_n, hn.data(), nc * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    SKC_CUDA(cudaMemcpyAsync(d_lists, hl.data(), nc * sizeof(void*), cudaMemcpyHostToDevice, s));
-    for (uint32_t g0 = 0; g0 < nc; g0 += G) {
-      const uint32_t ng = std::min(G, nc - g0);
-      SKC_CUDA(cudaMemsetAsync(cnt, 0, ng * sizeof(uint32_t), s));
-      LvArgs a{ng, d_masks + g0, d_lists + g0, d_n + g0, (uint32_t)maxn, lv_cells, ds->x,
-               ds->n_pad, pr_c, pr_v, pr_n, cap, cnt, surv_id, surv_key, srt,
-               slot + (uint64_t)g0 * kLvSlot,
-               outs + g0, outs + nc + g0, outs + 2ull * nc + g0};
-      SKC_TRY(launch_lv_filter(s, a));
-      SKC_TRY(launch_lv_sfs(s, a));
+  }
+  const uint32_t n_items = (uint32_t)it_cub.size(), n_ph = (uint32_t)ph_size.size();
+
+  // 3. Device tables and scratch.
+  LtArgs a{};
+  LtJob* d_jobs;
+  uint32_t *d_mask, *d_job, *d_scr, *d_list_n, *d_nsky, *d_next, *d_flag, *d_slot;
+  const uint32_t** d_list;
+  SKC_TRY(A.alloc(&d_jobs, nj));
+  SKC_TRY(A.alloc(&d_mask, ncub));
+  SKC_TRY(A.alloc(&d_job, ncub));
+  SKC_TRY(A.alloc(&d_scr, ncub));
+  SKC_TRY(A.alloc(&d_list, ncub));
+  SKC_TRY(A.alloc(&d_list_n, ncub));
+  SKC_TRY(A.alloc(&d_nsky, ncub));
+  SKC_TRY(A.alloc(&d_next, ncub));
+  SKC_TRY(A.alloc(&d_flag, ncub));
+  SKC_TRY(A.alloc(&d_slot, (uint64_t)ncub * kLvSlot));
+  SKC_TRY(A.alloc(&a.pr_c, (uint64_t)g_used * kLvPruners));
+  SKC_TRY(A.alloc(&a.pr_v, (uint64_t)g_used * kLvMaxDims * kLvPruners));
+  SKC_TRY(A.alloc(&a.pr_n, g_used));
+  SKC_TRY(A.alloc(&a.cnt, g_used));
+  SKC_TRY(A.alloc(&a.surv_id, (uint64_t)g_used * cap));
+  SKC_TRY(A.alloc(&a.surv_key, (uint64_t)g_used * cap));
+  SKC_TRY(A.alloc(&a.srt, (uint64_t)g_used * cap));
+  uint32_t *d_it_cub, *d_it_arg, *d_it_phase, *d_ph_size, *d_counters;
+  uint8_t* d_ph_kind;
+  SKC_TRY(A.alloc(&d_it_cub, n_items));
+  SKC_TRY(A.alloc(&d_it_arg, n_items));
+  SKC_TRY(A.alloc(&d_it_phase, n_items));
+  SKC_TRY(A.alloc(&d_ph_size, n_ph));
+  SKC_TRY(A.alloc(&d_ph_kind, n_ph));
+  // counters: [0, n_ph) phase done, n_ph next item, n_ph + 1 status,
+  // then per job the first-level overflows
+  SKC_TRY(A.alloc(&d_counters, n_ph + 2 + nj));
+  SKC_TRY(copy_h2d(d_jobs, hjobs.data(), nj * sizeof(LtJob), s));
+  SKC_TRY(copy_h2d(d_mask, c_mask.data(), ncub * 4, s));
+  SKC_TRY(copy_h2d(d_job, c_job.data(), ncub * 4, s));
+  SKC_TRY(copy_h2d(d_scr, c_scr.data(), ncub * 4, s));
+  SKC_TRY(copy_h2d(d_it_cub, it_cub.data(), (size_t)n_items * 4, s));
+  SKC_TRY(copy_h2d(d_it_arg, it_arg.data(), (size_t)n_items * 4, s));
+  SKC_TRY(copy_h2d(d_it_phase, it_phase.data(), (size_t)n_items * 4, s));
+  SKC_TRY(copy_h2d(d_ph_size, ph_size.data(), n_ph * 4, s));
+  SKC_TRY(copy_h2d(d_ph_kind, ph_kind.data(), n_ph, s));
+  SKC_CUDA(cudaMemsetAsync(d_counters, 0, (n_ph + 2 + nj) * 4, s));
+  SKC_CUDA(cudaMemsetAsync(d_flag, 0, ncub * 4, s));
+  a.jobs = d_jobs;
+  a.c_mask = d_mask;
+  a.c_job = d_job;
+  a.c_scr = d_scr;
+  a.c_list = d_list;
+  a.c_list_n = d_list_n;
+  a.c_nsky = d_nsky;
+  a.c_next = d_next;
+  a.c_flag = d_flag;
+  a.slot = d_slot;
+  a.cap = cap;
+  a.n_items = n_items;
+  a.it_cub = d_it_cub;
+  a.it_arg = d_it_arg;
+  a.it_phase = d_it_phase;
+  a.ph_size = d_ph_size;
+  a.ph_kind = d_ph_kind;
+  a.ph_done = d_counters;
+  a.next_item = d_counters + n_ph;
+  a.status = d_counters + n_ph + 1;
+  a.job_over = d_counters + n_ph + 2;
+  a.max_fallbacks = kLvMaxFallbacks;
+  SKC_TRY(launch_lattice(s, ctx->num_sms, a));
+
+  std::vector<uint32_t> h_nsky(ncub), h_next(ncub), h_flag(ncub), h_tail(2 + nj);
+  SKC_TRY(copy_d2h(h_nsky.data(), d_nsky, ncub * 4, s));
+  SKC_TRY(copy_d2h(h_next.data(), d_next, ncub * 4, s));
+  SKC_TRY(copy_d2h(h_flag.data(), d_flag, ncub * 4, s));
+  SKC_TRY(copy_d2h(h_tail.data(), d_counters + n_ph, (2 + nj) * 4, s));
+  if (h_tail[1]) return set_error(SKC_ERR_TIMEOUT, "lattice kernel: a phase wait ran out");
+  T.mark("lattice kernel");
+
+  // 4. Per job: host fallbacks for cuboids over a capacity, then the CSRs.
+  for (uint32_t j = 0; j < nj; ++j) {
+    LatticeJob& J = jobs[j];
+    if (h_tail[2 + j] > (uint32_t)kLvMaxFallbacks) {
+      J.status = kLvGiveUp;
+      continue;
     }
-    std::vector<uint32_t> h(3ull * nc);
-    SKC_CUDA(cudaMemcpyAsync(h.data(), outs, 3ull * nc * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    SKC_CUDA(cudaStreamSynchronize(s));  // also keeps the uploaded host vectors alive
-    if (lev == max_d) {
-      int over = 0;
-      for (uint32_t i = 0; i < nc; ++i) over += h[2ull * nc + i] != 0;
-      if (over > kLvMaxFallbacks) return kLvGiveUp;
-    }
-    for (uint32_t i = 0; i < nc; ++i) {
-      const uint32_t c = cubs[i];
-      if (h[2ull * nc + i] == 0) {
-        sky[c] = slot + (uint64_t)i * kLvSlot;
-        nsky[c] = h[i];
+    skc_dataset* ds = J.ds;
+    const int d = ds->d;
+    const uint32_t nsub = 1u << d, full = nsub - 1;
+    FullSpace& F = *J.F;
+    std::vector<uint32_t*> sky(nsub, nullptr), ext(nsub, nullptr);
+    std::vector<uint64_t> nsky(nsub, 0), next(nsub, 0);
+    sky[full] = F.sky;
+    ext[full] = F.ext;
+    nsky[full] = F.h_counts[0];
+    next[full] = F.h_counts[1];
+    CuboidScratch cs;
+    bool cs_ready = false;
+    int fallbacks = 0;
+    for (uint32_t i = 0; i < (uint32_t)J.masks.size(); ++i) {
+      const uint32_t c = J.masks[i], t = J.cub0 + i;
+      if (h_flag[t] == 0) {
+        sky[c] = d_slot + (uint64_t)t * kLvSlot;
+        nsky[c] = h_nsky[t];
         ext[c] = sky[c] + nsky[c];
-        next[c] = h[nc + i];
-        lst[c] = sky[c];
-        done[c] = 1;
+        next[c] = h_next[t];
         continue;
       }
-      // Over a capacity: the single-cuboid pipeline on an ascending list.
+      // Over a capacity: the single-cuboid pipeline on the full-space
+      // candidates (ascending, a superset of every cuboid's lists).
       if (!cs_ready) {
         SKC_TRY(cuboid_scratch(A, d, F.h_counts[2], &cs));
         cs_ready = true;
       }
       ++fallbacks;
-      const uint32_t p = src[i];
-      const uint64_t mc = nsky[p] + next[p];
-      const uint32_t* cand = F.cand;
-      if (p != full) {
-        SKC_TRY(launch_merge_disjoint(s, sky[p], (uint32_t)nsky[p], ext[p], (uint32_t)next[p], cs.cand));
-        cand = cs.cand;
-      }
-      SKC_TRY(cuboid_lists(E, ds, F, depth, A, cs, c, cand, mc, &sky[c], &ext[c], &nsky[c], &next[c]));
-      uint32_t* merged;
-      SKC_TRY(A.alloc(&merged, std::max<uint64_t>(1, nsky[c] + next[c])));
-      SKC_TRY(launch_merge_disjoint(s, sky[c], (uint32_t)nsky[c], ext[c], (uint32_t)next[c], merged));
-      lst[c] = merged;
-      done[c] = 1;
+      SKC_TRY(cuboid_lists(E, ds, F, J.depth, A, cs, c, F.cand, F.h_counts[2], &sky[c], &ext[c],
+                           &nsky[c], &next[c]));
     }
-    static const char* const kLevelMark[] = {"", "level 1", "level 2", "level 3", "level 4"};
-    T.mark(kLevelMark[lev]);
+    if (fallbacks) T.mark("lattice fallbacks");
+    J.R->level_fallbacks = fallbacks;
+    SKC_TRY(assemble_csr(E, A, d, J.max_d, J.want_ext, sky, nsky, ext, next, J.R));
   }
-  R->level_fallbacks = fallbacks;
-  const bool want_ext = o.want_extended || o.algo == SKC_ALGO_SDSC;
-  return assemble_csr(E, A, d, max_d, want_ext, sky, nsky, ext, next, R);
+  return SKC_OK;
+}
+
+static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d, int depth,
+                      Arena& A, FullSpace& F, skc_result* R, Tracer& T) {
+  std::vector<LatticeJob> jobs(1);
+  jobs[0].ds = ds;
+  jobs[0].max_d = max_d;
+  jobs[0].depth = depth;
+  jobs[0].want_ext = o.want_extended || o.algo == SKC_ALGO_SDSC;
+  jobs[0].F = &F;
+  jobs[0].R = R;
+  SKC_TRY(run_lattice(E, jobs, A, T));
+  return jobs[0].status;
 }
 
 // The level form replaces the bitmaps for batched capped skycubes of small
@@ -869,8 +1085,7 @@ static bool use_levels(const Exec& E, const skc_dataset* ds, const skc_options& 
                        const FullSpace& F) {
   if (o.form == SKC_FORM_BITMAPS) return false;
   const bool can = !E.plan && o.mode == SKC_MODE_BATCHED && !o.want_bitmaps &&
-                   max_d <= kLvMaxDims && max_d <= ds->d - 2 && ds->n < (1ull << 31) &&
-                   F.h_counts[2] <= 65535ull * kLvChunk;  // filter grid's y extent
+                   max_d <= kLvMaxDims && max_d <= ds->d - 2 && ds->n < (1ull << 31);
   return can && (o.form == SKC_FORM_LEVELS || F.h_counts[2] >= kLvMinCandidates);
 }
 
@@ -907,8 +1122,7 @@ static int dataset_signature(skc_dataset* ds, cudaStream_t s, uint32_t sig[3]) {
     uint32_t* out;
     SKC_TRY(A.alloc(&out, 3));
     SKC_TRY(launch_sample_signature(s, ds->x, ds->n_pad, ds->n, ds->d, out));
-    SKC_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s));
-    SKC_CUDA(cudaStreamSynchronize(s));
+    SKC_TRY(copy_d2h(h, out, sizeof(h), s));
   }
   std::lock_guard<std::mutex> lock(ctx->mu);
   ds->sig_samples = h[2];
@@ -1204,16 +1418,13 @@ static int upload_on(skc_context* ctx, cudaStream_t s, const float* rows, uint64
     if (from_host) {
       float* tmp;
       if ((st = A.alloc(&tmp, n * d)) != SKC_OK) break;
-      e = cudaMemcpyAsync(tmp, rows, n * d * sizeof(float), cudaMemcpyHostToDevice, s);
-      if (e != cudaSuccess) { st = set_error(SKC_ERR_CUDA, "upload copy failed: %s", cudaGetErrorString(e)); break; }
+      if ((st = copy_h2d(tmp, rows, n * d * sizeof(float), s)) != SKC_OK) break;
       d_rows = tmp;
     }
     if ((st = A.alloc(&bad, 1)) != SKC_OK) break;
     if (cudaMemsetAsync(bad, 0, sizeof(uint32_t), s) != cudaSuccess) { st = set_error(SKC_ERR_CUDA, "memset"); break; }
     if ((st = launch_rows_to_soa(s, d_rows, n, d, ds->n_pad, ds->x, bad)) != SKC_OK) break;
-    e = cudaMemcpyAsync(&h_bad, bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) { st = set_error(SKC_ERR_CUDA, "upload failed: %s", cudaGetErrorString(e)); break; }
+    if ((st = copy_d2h(&h_bad, bad, sizeof(uint32_t), s)) != SKC_OK) break;
     if (h_bad) st = set_error(SKC_ERR_INVALID, "%u non-finite attribute values (NaN/inf) rejected", h_bad);
   } while (0);
   if (st != SKC_OK) {
@@ -1354,8 +1565,7 @@ static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, const RunPara
     SKC_TRY(launch_partition_skyline(s, d, depth, LT, pa, ps));
     SKC_TRY(launch_status_compact(s, status, list, m_ptr, m, 0, blk0, blk1, sky, ext, cnt, cnt + 1));
     uint32_t h[2] = {0, 0};
-    SKC_CUDA(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s));
-    SKC_CUDA(cudaStreamSynchronize(s));
+    SKC_TRY(copy_d2h(h, cnt, sizeof(h), s));
     nsky = h[0];
     next = h[1];
     T.mark("subspace skyline");
@@ -1366,7 +1576,7 @@ static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, const RunPara
     for (uint32_t c = 0; c < nsub; ++c) off[c + 1] = off[c] + (c == S ? cntc : 0);
     uint64_t* d_off;
     SKC_TRY(A.alloc(&d_off, nsub + 1));
-    SKC_CUDA(cudaMemcpyAsync(d_off, off.data(), (nsub + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    SKC_TRY(copy_h2d(d_off, off.data(), (nsub + 1) * sizeof(uint64_t), s));
     SKC_CUDA(cudaStreamSynchronize(s));  // `off` is a host temporary
     uint32_t* ids = pass == 0 ? sky : ext;
     A.release(d_off);
@@ -1710,11 +1920,10 @@ int skc_dataset_update(skc_dataset* ds, const float* rows) {
     SKC_TRY(A.alloc(&tmp, n * d));
     SKC_TRY(A.alloc(&soa, (uint64_t)d * ds->n_pad));
     SKC_TRY(A.alloc(&bad, 1));
-    SKC_CUDA(cudaMemcpyAsync(tmp, rows, n * d * sizeof(float), cudaMemcpyHostToDevice, s));
+    SKC_TRY(copy_h2d(tmp, rows, n * d * sizeof(float), s));
     SKC_CUDA(cudaMemsetAsync(bad, 0, sizeof(uint32_t), s));
     SKC_TRY(launch_rows_to_soa(s, tmp, n, d, ds->n_pad, soa, bad));
-    SKC_CUDA(cudaMemcpyAsync(&h_bad, bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    SKC_CUDA(cudaStreamSynchronize(s));
+    SKC_TRY(copy_d2h(&h_bad, bad, sizeof(uint32_t), s));
     if (!h_bad) {
       // The dataset may live on another stream: order the copy after it.
       if (ds->stream && ds->stream != s) SKC_CUDA(cudaStreamSynchronize(ds->stream));
@@ -1915,12 +2124,9 @@ static int download_csr(skc_result* r, bool ext) {
   cudaStream_t s = r->stream;
   SKC_CUDA(cudaSetDevice(r->ctx->device));
   off.resize(nsub + 1);
-  SKC_CUDA(cudaMemcpyAsync(off.data(), d_off, (nsub + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-  SKC_CUDA(cudaStreamSynchronize(s));
+  SKC_TRY(copy_d2h(off.data(), d_off, (nsub + 1) * sizeof(uint64_t), s));
   take_host_buffer(r->ctx, ids, off[nsub]);
-  if (off[nsub])
-    SKC_CUDA(cudaMemcpyAsync(ids.data(), d_ids, off[nsub] * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  SKC_CUDA(cudaStreamSynchronize(s));
+  SKC_TRY(copy_d2h(ids.data(), d_ids, off[nsub] * sizeof(uint32_t), s));
   done = true;
   return SKC_OK;
 }
@@ -1971,8 +2177,8 @@ int skc_result_bitmaps(skc_result* r, const uint32_t** bits, const uint32_t** pi
     r->h_bits.resize(r->n_cand * r->words);
     r->h_cand.resize(r->n_cand);
     if (r->n_cand) {
-      SKC_CUDA(cudaMemcpyAsync(r->h_bits.data(), r->d_bits, r->h_bits.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-      SKC_CUDA(cudaMemcpyAsync(r->h_cand.data(), r->d_cand, r->n_cand * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      SKC_TRY(copy_d2h(r->h_bits.data(), r->d_bits, r->h_bits.size() * sizeof(uint32_t), s));
+      SKC_TRY(copy_d2h(r->h_cand.data(), r->d_cand, r->n_cand * sizeof(uint32_t), s));
     }
     SKC_CUDA(cudaStreamSynchronize(s));
     r->bits_downloaded = true;
@@ -2026,6 +2232,7 @@ struct Request {
   int d = 0;
   skc_options opt{};
   uint64_t footprint = 0;
+  bool heavy = false;  // runs on the slot's low-priority stream
   std::chrono::steady_clock::time_point t_submit, t_start, t_end;
   bool done = false;
   bool claimed = false;  // a skc_server_wait has taken this ticket
@@ -2047,7 +2254,10 @@ struct skc_server {
   uint64_t in_use = 0;
   int slots = 0;
   std::vector<std::thread> workers;
-  std::vector<cudaStream_t> streams;
+  // Per slot: a high-priority stream for light requests and a low-priority
+  // one for heavy requests, so a light request's kernels are dispatched
+  // ahead of a heavy one's pending work.
+  std::vector<cudaStream_t> streams, streams_lo;
   std::deque<std::shared_ptr<Request>> queue;
   std::map<uint64_t, std::shared_ptr<Request>> tickets;
   std::mutex mu;
@@ -2105,6 +2315,13 @@ static int result_to_host(skc_result* r) {
   return SKC_OK;
 }
 
+// Heavy requests: the per-point bitmaps of many candidates over many
+// subspaces (about n * 2^d >= 2^29: 8k points at d = 16, 512k at d = 10).
+static bool heavy_request(uint64_t n, int d, const skc_options& o) {
+  if (o.subspace) return false;
+  return (n << d) >= (1ull << 29);
+}
+
 static void serve_one(skc_server* S, cudaStream_t stream, Request& q) {
   clear_error();
   Exec E;
@@ -2129,7 +2346,6 @@ static void serve_one(skc_server* S, cudaStream_t stream, Request& q) {
 
 static void worker_loop(skc_server* S, int slot) {
   cudaSetDevice(S->ctx->device);
-  cudaStream_t stream = S->streams[slot];
   for (;;) {
     std::shared_ptr<Request> q;
     {
@@ -2147,7 +2363,7 @@ static void worker_loop(skc_server* S, int slot) {
       S->peak_in_flight = std::max(S->peak_in_flight, S->in_flight);
       q->t_start = std::chrono::steady_clock::now();
     }
-    serve_one(S, stream, *q);
+    serve_one(S, q->heavy ? S->streams_lo[slot] : S->streams[slot], *q);
     {
       std::lock_guard<std::mutex> lk(S->mu);
       S->in_use -= q->footprint;
@@ -2177,14 +2393,20 @@ int skc_server_create(skc_context* ctx, int slots, uint64_t budget, skc_server**
   S->ctx = ctx;
   S->budget = budget;
   S->slots = slots;
+  int prio_lo = 0, prio_hi = 0;
+  SKC_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
   for (int i = 0; i < slots; ++i) {
-    cudaStream_t st;
-    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStream_t hi = nullptr, lo = nullptr;
+    if (cudaStreamCreateWithPriority(&hi, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&lo, cudaStreamNonBlocking, prio_lo) != cudaSuccess) {
+      if (hi) cudaStreamDestroy(hi);
       for (auto x : S->streams) cudaStreamDestroy(x);
+      for (auto x : S->streams_lo) cudaStreamDestroy(x);
       delete S;
       return set_error(SKC_ERR_CUDA, "stream creation failed");
     }
-    S->streams.push_back(st);
+    S->streams.push_back(hi);
+    S->streams_lo.push_back(lo);
   }
   for (int i = 0; i < slots; ++i) S->workers.emplace_back(worker_loop, S, i);
   *out = S;
@@ -2225,6 +2447,7 @@ int skc_server_submit(skc_server* S, const float* rows, uint64_t n, int d, const
   if (q->opt.subspace >= (1u << d))
     return set_error(SKC_ERR_INVALID, "subspace 0x%x has attributes beyond d=%d", q->opt.subspace, d);
   q->footprint = footprint_estimate(n, d, q->opt, true);
+  q->heavy = heavy_request(n, d, q->opt);
   return submit_common(S, q, ticket);
 }
 
@@ -2240,6 +2463,7 @@ int skc_server_submit_dataset(skc_server* S, skc_dataset* ds, const skc_options*
   skc_options_init(&q->opt);
   if (opt) q->opt = *opt;
   q->footprint = footprint_estimate(ds->n, ds->d, q->opt, false);
+  q->heavy = heavy_request(ds->n, ds->d, q->opt);
   return submit_common(S, q, ticket);
 }
 
@@ -2301,6 +2525,7 @@ int skc_server_destroy(skc_server* S) {
   for (auto& kv : S->tickets)
     if (kv.second->result) skc_result_free(kv.second->result);
   for (auto st : S->streams) cudaStreamDestroy(st);
+  for (auto st : S->streams_lo) cudaStreamDestroy(st);
   delete S;
   return SKC_OK;
 }

@@ -230,32 +230,54 @@ constexpr uint32_t kLvExt = 4096;      // extended-skyline points per cuboid
 constexpr uint32_t kLvSlot = kLvWin + kLvExt;  // output ids per cuboid
 constexpr uint32_t kLvSortCap = 8192;  // power of two >= kLvSlot
 constexpr uint32_t kLvKeyBins = 127 * kLvMaxDims + 1;  // cell sums
-struct LvArgs {
-  uint32_t ncub;                 // cuboids of this launch
-  const uint32_t* masks;         // [ncub]
-  const uint32_t* const* lists;  // [ncub] candidate ids
-  const uint32_t* list_n;        // [ncub]
-  uint32_t max_list;             // upper bound of list_n
-  const uint4* cells;            // point id -> grid cells
-  const float* x;                // attribute-major points, pitch n_pad
+// One dataset of a lattice launch.
+struct LtJob {
+  const float* x;            // attribute-major points, pitch n_pad
   uint64_t n_pad;
-  uint32_t* pr_c;                // [ncub * kLvPruners] pruner cells (packed over S)
-  float* pr_v;                   // [ncub * kLvMaxDims * kLvPruners] pruner values
-  uint32_t* pr_n;                // [ncub] pruners per cuboid
-  uint32_t cap;                  // survivors kept per cuboid
-  uint32_t* cnt;                 // [ncub] survivors (zeroed before the filter)
-  uint32_t* surv_id;             // [ncub * cap]
-  uint16_t* surv_key;            // [ncub * cap]
-  uint32_t* srt;                 // [ncub * cap] survivors by cell sum
-  uint32_t* slot;                // [ncub * kLvSlot]: skyline ids, then extended
-  uint32_t* o_nsky;              // [ncub]
-  uint32_t* o_next;              // [ncub]
-  uint32_t* o_flag;              // [ncub] 1: over a capacity, not computed
+  const uint4* cells;        // point id -> cells on the candidates' quantile grid
+  const uint32_t* cand;      // full-space skyline + extended skyline ids
+  uint32_t n_cand;
+  const uint32_t* cub_index; // [2^d] mask -> cuboid table index (0xffffffff: none)
+  int d, max_d;
 };
-int launch_lv_filter(cudaStream_t s, const LvArgs& a);
+// A lattice launch (levels.cu, k_lattice): every wanted cuboid of every job
+// (cuboid table index c) from a device work queue in lattice-level order.
+struct LtArgs {
+  const LtJob* jobs;
+  const uint32_t* c_mask;    // [ncub]
+  const uint32_t* c_job;     // [ncub]
+  const uint32_t* c_scr;     // [ncub] scratch index in the cuboid's group
+  const uint32_t** c_list;   // [ncub] candidate list (set by phase P)
+  uint32_t* c_list_n;        // [ncub]
+  uint32_t* c_nsky;          // [ncub] outputs of phase S
+  uint32_t* c_next;          // [ncub]
+  uint32_t* c_flag;          // [ncub] 1: over a capacity; 2: skipped (job handed over)
+  uint32_t* slot;            // [ncub * kLvSlot]: skyline ids, then extended
+  uint32_t* pr_c;            // [G * kLvPruners] per scratch index
+  float* pr_v;               // [G * kLvMaxDims * kLvPruners]
+  uint32_t* pr_n;            // [G]
+  uint32_t cap;              // survivors kept per cuboid
+  uint32_t* cnt;             // [G]
+  uint32_t* surv_id;         // [G * cap]
+  uint16_t* surv_key;        // [G * cap]
+  uint32_t* srt;             // [G * cap]
+  uint32_t n_items;
+  const uint32_t* it_cub;    // [n_items]
+  const uint32_t* it_arg;    // [n_items] phase F: slice | slices << 16
+  const uint32_t* it_phase;  // [n_items]
+  const uint32_t* ph_size;   // [n_phases] items per phase
+  const uint8_t* ph_kind;    // [n_phases] 0 P, 1 F, 2 S
+  uint32_t* ph_done;         // [n_phases] zeroed before the launch
+  uint32_t* next_item;       // zeroed before the launch
+  uint32_t* job_over;        // [jobs] first-level cuboids over a capacity (zeroed)
+  uint32_t max_fallbacks;    // more than this on a job's first level: job handed over
+  uint32_t* status;          // 0, or 1 when a wait ran out (zeroed)
+};
+// One cooperative launch of the lattice kernel on `num_sms` SMs.
+int launch_lattice(cudaStream_t s, int num_sms, const LtArgs& a);
+int lattice_grid(int num_sms, int* grid);
 int launch_scatter_u4(cudaStream_t s, const uint4* in, const uint32_t* idx, const uint32_t* m_ptr,
                       uint64_t m_max, uint4* out);
-int launch_lv_sfs(cudaStream_t s, const LvArgs& a);
 
 void upload_submask_table();
 

@@ -103,7 +103,6 @@ __device__ __forceinline__ int lv_dom(uint32_t qc, const float* qv, uint32_t pc,
 // they leave are staged and tested densely against the others, so a warp
 // runs the long pruner loop only on entries that need it.
 constexpr uint32_t kLvFirstPruners = 4;
-static constexpr size_t kLvFilterSmem = (size_t)kLvChunk * (4 + 4 + 4 + 2);
 
 // True when one of the pruners [j0, j1) strictly dominates p on S.
 __device__ __forceinline__ bool lv_pruned(uint32_t pc, uint32_t id, uint32_t j0, uint32_t j1,
@@ -130,36 +129,40 @@ __device__ __forceinline__ bool lv_pruned(uint32_t pc, uint32_t id, uint32_t j0,
   return false;
 }
 
-// Pruners of each cuboid: the lowest cell sums over S of a strided sample
-// of its list, selected once per cuboid for all its filter CTAs.
-__global__ void __launch_bounds__(256) k_lv_pruners(
-    const uint32_t* __restrict__ masks, const uint32_t* const* __restrict__ lists,
-    const uint32_t* __restrict__ list_n, const uint4* __restrict__ cells,
-    const float* __restrict__ x, uint64_t n_pad, uint32_t* __restrict__ pr_c_g,
-    float* __restrict__ pr_v_g, uint32_t* __restrict__ pr_n_g) {
-  __shared__ uint32_t hist[kLvKeyBins];
+// Data written inside the persistent kernel by other CTAs (pruners, lists,
+// survivors, parent slots, counts) is read through L2 (ld.global.cg), never
+// through the read-only or L1 paths, which are not coherent across SMs.
+__device__ __forceinline__ uint32_t ld_l2(const uint32_t* p) { return __ldcg(p); }
+__device__ __forceinline__ float ld_l2(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ uint16_t ld_l2(const uint16_t* p) {
+  return __ldcg(reinterpret_cast<const unsigned short*>(p));
+}
+
+// Pruners of cuboid S over its list L[0, n): the lowest cell sums over S of a
+// strided kLvSample-entry sample, into pr_c/pr_v/pr_n at scratch index g.
+// One CTA of kLvThreads threads (kLvSample / kLvThreads entries each).
+__device__ void lv_pruners_cta(const CubAttrs& A, const uint32_t* L, uint32_t n,
+                               const uint4* __restrict__ cells, const float* __restrict__ x,
+                               uint64_t n_pad, uint32_t g, uint32_t* pr_c_g, float* pr_v_g,
+                               uint32_t* pr_n_g, uint32_t* hist) {
   __shared__ uint32_t s_thr, s_np;
-  const uint32_t c = blockIdx.x;
-  const uint32_t n = list_n[c];
   const int tid = threadIdx.x;
   if (n == 0) {  // uniform over the CTA
-    if (tid == 0) pr_n_g[c] = 0;
+    if (tid == 0) pr_n_g[g] = 0;
     return;
   }
-  const uint32_t* __restrict__ L = lists[c];
-  const CubAttrs A = cub_attrs(masks[c]);
   const uint32_t ns = min(n, kLvSample);
   for (uint32_t i = tid; i < kLvKeyBins; i += blockDim.x) hist[i] = 0;
   __syncthreads();
-  constexpr int kPer = kLvSample / 256;
+  constexpr int kPer = (kLvSample + kLvThreads - 1) / kLvThreads;
   uint32_t sid[kPer], skey[kPer];
 #pragma unroll
   for (int r = 0; r < kPer; ++r) {
-    const uint32_t i = tid + 256u * r;
+    const uint32_t i = tid + kLvThreads * r;
     sid[r] = 0;
     skey[r] = 0xffffffffu;
     if (i < ns) {
-      sid[r] = L[(uint64_t)i * n / ns];
+      sid[r] = ld_l2(L + (uint64_t)i * n / ns);
       skey[r] = lv_key(lv_pack(cells[sid[r]], A));
       atomicAdd(&hist[skey[r]], 1u);
     }
@@ -186,55 +189,53 @@ __global__ void __launch_bounds__(256) k_lv_pruners(
       if (take) {
         const uint32_t k = atomicAdd(&s_np, 1u);
         if (k < kLvPruners) {
-          pr_c_g[(uint64_t)c * kLvPruners + k] = lv_pack(cells[sid[r]], A);
+          pr_c_g[(uint64_t)g * kLvPruners + k] = lv_pack(cells[sid[r]], A);
           float v[kLvMaxDims];
           lv_load(x, n_pad, sid[r], A, v);
 #pragma unroll
           for (int a = 0; a < kLvMaxDims; ++a)
-            pr_v_g[((uint64_t)c * kLvMaxDims + a) * kLvPruners + k] = v[a];
+            pr_v_g[((uint64_t)g * kLvMaxDims + a) * kLvPruners + k] = v[a];
         }
       }
     }
     __syncthreads();
   }
-  if (tid == 0) pr_n_g[c] = min(s_np, kLvPruners);
+  if (tid == 0) pr_n_g[g] = min(s_np, kLvPruners);
 }
 
-__global__ void __launch_bounds__(256) k_lv_filter(
-    const uint32_t* __restrict__ masks, const uint32_t* const* __restrict__ lists,
-    const uint32_t* __restrict__ list_n, const uint4* __restrict__ cells,
-    const float* __restrict__ x, uint64_t n_pad, const uint32_t* __restrict__ pr_c_g,
-    const float* __restrict__ pr_v_g, const uint32_t* __restrict__ pr_n_g, uint32_t cap,
-    uint32_t* __restrict__ cnt, uint32_t* __restrict__ surv_id, uint16_t* __restrict__ surv_key) {
+// Shared memory of one filter chunk, in bytes.
+static constexpr size_t kLvFilterSmem = (size_t)kLvChunk * (4 + 4 + 4 + 2);
+
+// The pruner filter of list entries [beg, end) of cuboid S (scratch index g):
+// every entry meets the first kLvFirstPruners pruners, the ones left are
+// staged and meet the others densely; survivors are appended to g's scratch
+// (one atomic per CTA). `sm` holds kLvFilterSmem bytes.
+__device__ void lv_filter_chunk(const CubAttrs& A, const uint32_t* L, uint32_t beg, uint32_t end,
+                                const uint4* __restrict__ cells, const float* __restrict__ x,
+                                uint64_t n_pad, uint32_t g, const uint32_t* pr_c_g,
+                                const float* pr_v_g, const uint32_t* pr_n_g, uint32_t cap,
+                                uint32_t* cnt, uint32_t* surv_id, uint16_t* surv_key,
+                                unsigned char* sm) {
   __shared__ uint32_t s_n1, s_n, s_base;
   __shared__ uint32_t pr_c[kLvPruners];
   __shared__ float pr_v[kLvMaxDims][kLvPruners];
-  extern __shared__ __align__(16) unsigned char lvf_smem[];
-  uint32_t* s1_id = reinterpret_cast<uint32_t*>(lvf_smem);  // [kLvChunk] staged entries
-  uint32_t* s1_pc = s1_id + kLvChunk;                        // [kLvChunk]
-  uint32_t* st_id = s1_pc + kLvChunk;                        // [kLvChunk] survivors
+  uint32_t* s1_id = reinterpret_cast<uint32_t*>(sm);          // [kLvChunk] staged entries
+  uint32_t* s1_pc = s1_id + kLvChunk;                          // [kLvChunk]
+  uint32_t* st_id = s1_pc + kLvChunk;                          // [kLvChunk] survivors
   uint16_t* st_key = reinterpret_cast<uint16_t*>(st_id + kLvChunk);  // [kLvChunk]
-  // Consecutive CTAs take different cuboids, spreading the appends.
-  const uint32_t c = blockIdx.x;
-  const uint32_t n = list_n[c];
-  const uint32_t beg = blockIdx.y * kLvChunk;
-  if (beg >= n) return;  // uniform over the CTA
-  const uint32_t end = min(n, beg + kLvChunk);
-  const uint32_t* __restrict__ L = lists[c];
-  const CubAttrs A = cub_attrs(masks[c]);
   const int tid = threadIdx.x, lane = tid & 31;
   if (tid < (int)kLvPruners) {
-    pr_c[tid] = pr_c_g[(uint64_t)c * kLvPruners + tid];
+    pr_c[tid] = ld_l2(pr_c_g + (uint64_t)g * kLvPruners + tid);
 #pragma unroll
     for (int a = 0; a < kLvMaxDims; ++a)
-      pr_v[a][tid] = pr_v_g[((uint64_t)c * kLvMaxDims + a) * kLvPruners + tid];
+      pr_v[a][tid] = ld_l2(pr_v_g + ((uint64_t)g * kLvMaxDims + a) * kLvPruners + tid);
   }
   if (tid == 0) {
     s_n1 = 0;
     s_n = 0;
   }
   __syncthreads();
-  const uint32_t np = pr_n_g[c];
+  const uint32_t np = ld_l2(pr_n_g + g);
   const uint32_t np1 = min(np, kLvFirstPruners);
 
   // Phase 1: every entry against the first pruners; the rest are staged.
@@ -245,7 +246,7 @@ __global__ void __launch_bounds__(256) k_lv_filter(
     uint32_t id = 0, pc = 0;
     bool keep = false;
     if (valid) {
-      id = L[i];
+      id = ld_l2(L + i);
       pc = lv_pack(cells[id], A);
       keep = !lv_pruned(pc, id, 0, np1, pr_c, pr_v, x, n_pad, A);
     }
@@ -272,19 +273,20 @@ __global__ void __launch_bounds__(256) k_lv_filter(
   }
   __syncthreads();
   const uint32_t ns_kept = s_n;
-  if (tid == 0) s_base = ns_kept ? atomicAdd(&cnt[c], ns_kept) : 0u;
+  if (tid == 0) s_base = ns_kept ? atomicAdd(&cnt[g], ns_kept) : 0u;
   __syncthreads();
   const uint32_t b0 = s_base;
   for (uint32_t k = tid; k < ns_kept; k += blockDim.x) {
     const uint32_t pos = b0 + k;
     if (pos < cap) {
-      surv_id[(uint64_t)c * cap + pos] = st_id[k];
-      surv_key[(uint64_t)c * cap + pos] = st_key[k];
+      surv_id[(uint64_t)g * cap + pos] = st_id[k];
+      surv_key[(uint64_t)g * cap + pos] = st_key[k];
     }
   }
+  __syncthreads();  // the staging arrays are reused by the next chunk
 }
 
-// Shared memory of k_lv_sfs, in bytes.
+// Shared memory of the sort-filter skyline of one cuboid, in bytes.
 static constexpr size_t kLvSfsSmem =
     (2 * (kLvKeyBins + 1)) * 4 +                                   // bucket offsets, cursors
     kLvWin * (4 + 4 * kLvMaxDims + 4 + 1) +                        // window
@@ -292,26 +294,28 @@ static constexpr size_t kLvSfsSmem =
     kLvThreads * (4 + 4 * kLvMaxDims + 4 + 2 + 1) +                // batch
     kLvSortCap * 4 + 64;                                           // sort buffer, counters
 
-__global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
-    const uint32_t* __restrict__ masks, const uint4* __restrict__ cells,
-    const float* __restrict__ x, uint64_t n_pad, uint32_t cap, const uint32_t* __restrict__ cnt,
-    const uint32_t* __restrict__ surv_id, const uint16_t* __restrict__ surv_key,
-    uint32_t* __restrict__ srt, uint32_t* __restrict__ slot, uint32_t* __restrict__ o_nsky,
-    uint32_t* __restrict__ o_next, uint32_t* __restrict__ o_flag) {
-  extern __shared__ __align__(16) unsigned char lv_smem[];
-  const uint32_t c = blockIdx.x;
+// The skyline and extended skyline of cuboid c over the survivors in
+// scratch index g, into c's slot (skyline ids, then extended ids, each
+// ascending) and o_nsky/o_next/o_flag[c]; o_flag[c] = 1 when a capacity is
+// exceeded (nothing computed: the host takes the cuboid). One CTA of
+// kLvThreads threads; `lv_smem` holds kLvSfsSmem bytes. Returns the flag.
+__device__ uint32_t lv_sfs_cta(const CubAttrs& A, uint32_t c, uint32_t g,
+                               const uint4* __restrict__ cells, const float* __restrict__ x,
+                               uint64_t n_pad, uint32_t cap, const uint32_t* cnt,
+                               const uint32_t* surv_id, const uint16_t* surv_key, uint32_t* srt,
+                               uint32_t* slot, uint32_t* o_nsky, uint32_t* o_next,
+                               uint32_t* o_flag, unsigned char* lv_smem) {
   const int tid = threadIdx.x;
-  const uint32_t n = cnt[c];
+  const uint32_t n = ld_l2(cnt + g);
   if (n > cap) {  // survivors beyond the scratch: the host takes this cuboid
     if (tid == 0) {
       o_flag[c] = 1;
       o_nsky[c] = 0;
       o_next[c] = 0;
     }
-    return;
+    return 1;
   }
-  const CubAttrs A = cub_attrs(masks[c]);
-  const uint64_t off = (uint64_t)c * cap;
+  const uint64_t off = (uint64_t)g * cap;
 
   uint32_t* kb = reinterpret_cast<uint32_t*>(lv_smem);   // [kLvKeyBins + 1]
   uint32_t* cur = kb + kLvKeyBins + 1;                    // [kLvKeyBins + 1]
@@ -336,7 +340,7 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
   for (uint32_t k = tid; k <= kLvKeyBins; k += blockDim.x) cur[k] = 0;
   if (tid < 8) ctr[tid] = 0;
   __syncthreads();
-  for (uint32_t i = tid; i < n; i += blockDim.x) atomicAdd(&cur[surv_key[off + i]], 1u);
+  for (uint32_t i = tid; i < n; i += blockDim.x) atomicAdd(&cur[ld_l2(surv_key + off + i)], 1u);
   __syncthreads();
   if (tid == 0) {
     uint32_t acc = 0;
@@ -350,8 +354,8 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
   for (uint32_t k = tid; k < kLvKeyBins; k += blockDim.x) cur[k] = kb[k];
   __syncthreads();
   for (uint32_t i = tid; i < n; i += blockDim.x) {
-    const uint32_t p = atomicAdd(&cur[surv_key[off + i]], 1u);
-    srt[off + p] = surv_id[off + i];
+    const uint32_t p = atomicAdd(&cur[ld_l2(surv_key + off + i)], 1u);
+    srt[off + p] = ld_l2(surv_id + off + i);
   }
   __syncthreads();
 
@@ -493,7 +497,8 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
       o_nsky[c] = 0;
       o_next[c] = 0;
     }
-    return;
+    __syncthreads();  // ctr is reused by the CTA's next item
+    return 1;
   }
 
   // 3. Later entries of the same cell sum with equal cells on S; a warp per
@@ -572,6 +577,8 @@ __global__ void __launch_bounds__(kLvThreads) k_lv_sfs(
     o_next[c] = kept - ctr[5];
     o_flag[c] = 0;
   }
+  __syncthreads();  // shared memory is reused by the CTA's next item
+  return 0;
 }
 
 // out[idx[i]] = in[i] for i < *m_ptr.
@@ -592,28 +599,164 @@ int launch_scatter_u4(cudaStream_t s, const uint4* in, const uint32_t* idx, cons
   return SKC_OK;
 }
 
-int launch_lv_filter(cudaStream_t s, const LvArgs& a) {
-  if (a.ncub == 0 || a.max_list == 0) return SKC_OK;
-  const dim3 grid(a.ncub, (unsigned)((a.max_list + kLvChunk - 1) / kLvChunk));
-  k_lv_pruners<<<a.ncub, 256, 0, s>>>(a.masks, a.lists, a.list_n, a.cells, a.x, a.n_pad,
-                                      a.pr_c, a.pr_v, a.pr_n);
-  SKC_LAUNCH_CHECK();
-  SKC_CUDA(cudaFuncSetAttribute(k_lv_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)kLvFilterSmem));
-  k_lv_filter<<<grid, 256, kLvFilterSmem, s>>>(a.masks, a.lists, a.list_n, a.cells, a.x, a.n_pad,
-                                               a.pr_c, a.pr_v, a.pr_n, a.cap, a.cnt, a.surv_id,
-                                               a.surv_key);
-  SKC_LAUNCH_CHECK();
+// ---------------------------------------------------------------------------
+// The lattice work queue: one persistent launch computes every wanted cuboid
+// of every job (dataset). Items sit in lattice-level order: for each level,
+// top down, and each group of cuboids that fits the survivor scratch, a
+// phase P (per cuboid: its smallest computed parent's skyline + extended
+// skyline as the candidate list, then its pruners), a phase F (per cuboid
+// and slice: the pruner filter of the slice's chunks) and a phase S (per
+// cuboid: the sort-filter skyline). A CTA pops the next item from a device
+// counter and, before running it, waits until every item of the previous
+// phase is done. Items are popped in order, so the items waited for are
+// running on resident CTAs (the launch is cooperative: every CTA is
+// resident); the waits are bounded and set status[0] when they run out.
+constexpr uint32_t kLtWaitLimit = 1u << 25;  // about 9 s of 256 ns sleeps
+
+__device__ __forceinline__ bool lt_wait_phase(const uint32_t* done, uint32_t want,
+                                              uint32_t* status) {
+  for (uint32_t it = 0; it < kLtWaitLimit; ++it) {
+    if (ld_l2(done) >= want) return true;
+    if (ld_l2(status) != 0) return false;
+    __nanosleep(256);
+  }
+  atomicExch(status, 1u);
+  return false;
+}
+
+// Candidate list of cuboid c: the computed parent (one more attribute,
+// within the job's cap, not the full space, not over a capacity) with the
+// smallest skyline + extended skyline, as findMinParent picks it, else the
+// job's full-space candidates. Any parent's list holds every point of c's
+// skyline and extended skyline and its dominators among them, so the choice
+// changes the work only.
+__device__ void lt_choose_list(const LtArgs& a, uint32_t c, const uint32_t** list,
+                               uint32_t* n) {
+  const LtJob& J = a.jobs[a.c_job[c]];
+  const uint32_t S = a.c_mask[c];
+  const uint32_t full = (1u << J.d) - 1u;
+  uint32_t best = 0xffffffffu, best_n = 0xffffffffu;
+  for (int k = J.d - 1; k >= 0; --k) {  // parents in generate_lattice's order
+    if (S & (1u << k)) continue;
+    const uint32_t P = S | (1u << k);
+    if (P == full || __popc(P) > J.max_d) continue;
+    const uint32_t pi = J.cub_index[P];
+    if (pi == 0xffffffffu || ld_l2(a.c_flag + pi) != 0) continue;
+    const uint32_t pn = ld_l2(a.c_nsky + pi) + ld_l2(a.c_next + pi);
+    if (pn < best_n) {
+      best_n = pn;
+      best = pi;
+    }
+  }
+  if (best == 0xffffffffu) {
+    *list = J.cand;
+    *n = J.n_cand;
+  } else {
+    *list = a.slot + (uint64_t)best * kLvSlot;
+    *n = best_n;
+  }
+}
+
+__global__ void __launch_bounds__(kLvThreads, 1) k_lattice(LtArgs a) {
+  extern __shared__ __align__(16) unsigned char lt_smem[];
+  __shared__ uint32_t s_item, s_run;
+  __shared__ const uint32_t* s_list;
+  __shared__ uint32_t s_n;
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) {
+      const uint32_t it = atomicAdd(a.next_item, 1u);
+      uint32_t run = 0;
+      if (it < a.n_items) {
+        const uint32_t ph = a.it_phase[it];
+        run = (ph == 0 || lt_wait_phase(a.ph_done + ph - 1, a.ph_size[ph - 1], a.status)) ? 1u : 0u;
+        if (run) {
+          // a job whose first level overflowed too often goes to the bitmap
+          // form: the host recomputes it, its remaining items only count
+          const uint32_t c = a.it_cub[it];
+          const uint32_t j = a.c_job[c];
+          if (ld_l2(a.job_over + j) > a.max_fallbacks) run = 2;
+        }
+      }
+      s_item = it;
+      s_run = run;
+    }
+    __syncthreads();
+    const uint32_t it = s_item;
+    if (it >= a.n_items) return;
+    const uint32_t ph = a.it_phase[it];
+    if (s_run == 1) {
+      const uint32_t c = a.it_cub[it];
+      const uint32_t g = a.c_scr[c];
+      const LtJob& J = a.jobs[a.c_job[c]];
+      const CubAttrs A = cub_attrs(a.c_mask[c]);
+      const uint32_t kind = a.ph_kind[ph];
+      if (kind == 0) {  // P: candidate list and pruners
+        if (tid == 0) {
+          const uint32_t* L;
+          uint32_t n;
+          lt_choose_list(a, c, &L, &n);
+          a.c_list[c] = L;
+          a.c_list_n[c] = n;
+          a.cnt[g] = 0;
+          s_list = L;
+          s_n = n;
+        }
+        __syncthreads();
+        lv_pruners_cta(A, s_list, s_n, J.cells, J.x, J.n_pad, g, a.pr_c, a.pr_v, a.pr_n,
+                       reinterpret_cast<uint32_t*>(lt_smem));
+      } else if (kind == 1) {  // F: chunks slice, slice + nslices, ... of the list
+        const uint32_t slice = a.it_arg[it] & 0xffffu, nsl = a.it_arg[it] >> 16;
+        const uint32_t* L = reinterpret_cast<const uint32_t*>(
+            __ldcg(reinterpret_cast<const unsigned long long*>(a.c_list + c)));
+        const uint32_t n = ld_l2(a.c_list_n + c);
+        for (uint32_t k = slice; (uint64_t)k * kLvChunk < n; k += nsl)
+          lv_filter_chunk(A, L, k * kLvChunk, min(n, (k + 1) * kLvChunk), J.cells, J.x, J.n_pad,
+                          g, a.pr_c, a.pr_v, a.pr_n, a.cap, a.cnt, a.surv_id, a.surv_key, lt_smem);
+      } else {  // S: the sort-filter skyline
+        const uint32_t over = lv_sfs_cta(A, c, g, J.cells, J.x, J.n_pad, a.cap, a.cnt, a.surv_id,
+                                         a.surv_key, a.srt, a.slot, a.c_nsky, a.c_next,
+                                         a.c_flag, lt_smem);
+        if (over && tid == 0 && __popc(a.c_mask[c]) == J.max_d)
+          atomicAdd(a.job_over + a.c_job[c], 1u);
+      }
+    } else if (s_run == 2 && a.ph_kind[ph] == 2 && tid == 0) {
+      const uint32_t c = a.it_cub[it];  // skipped: flagged for the host
+      a.c_flag[c] = 2;
+      a.c_nsky[c] = 0;
+      a.c_next[c] = 0;
+    }
+    // Publish: every thread's writes reach L2 before the phase counter moves.
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicAdd(a.ph_done + ph, 1u);
+  }
+}
+
+static size_t lattice_smem() {
+  return kLvSfsSmem > kLvFilterSmem ? kLvSfsSmem : kLvFilterSmem;
+}
+
+// Persistent CTAs of the lattice kernel on `num_sms` SMs (one per SM).
+int lattice_grid(int num_sms, int* grid) {
+  SKC_CUDA(cudaFuncSetAttribute(k_lattice, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)lattice_smem()));
+  int per_sm = 0;
+  SKC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lattice, kLvThreads,
+                                                         lattice_smem()));
+  if (per_sm < 1) return set_error(SKC_ERR_UNSUPPORTED, "the lattice kernel does not fit an SM");
+  *grid = per_sm * num_sms;
   return SKC_OK;
 }
 
-int launch_lv_sfs(cudaStream_t s, const LvArgs& a) {
-  if (a.ncub == 0) return SKC_OK;
-  SKC_CUDA(cudaFuncSetAttribute(k_lv_sfs, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)kLvSfsSmem));
-  k_lv_sfs<<<a.ncub, kLvThreads, kLvSfsSmem, s>>>(a.masks, a.cells, a.x, a.n_pad, a.cap, a.cnt,
-                                                  a.surv_id, a.surv_key, a.srt, a.slot, a.o_nsky,
-                                                  a.o_next, a.o_flag);
+int launch_lattice(cudaStream_t s, int num_sms, const LtArgs& a) {
+  if (a.n_items == 0) return SKC_OK;
+  int grid = 0;
+  SKC_TRY(lattice_grid(num_sms, &grid));
+  LtArgs args = a;
+  void* params[] = {&args};
+  SKC_CUDA(cudaLaunchCooperativeKernel((const void*)k_lattice, dim3(grid), dim3(kLvThreads),
+                                       params, lattice_smem(), s));
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }

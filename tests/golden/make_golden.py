@@ -96,12 +96,18 @@ def points_hash(x):
 DIGEST_CASES = ("anticorr-1m-10", "corrq-566k-15-m6", "uniform-100k-6", "ties-581k-10")
 
 
+# Down-scaled stand-ins of full-size workloads whose reference run takes too
+# long here: (distribution, n, d, max_d, seed), same generator and seed.
+SCALED = {"corrq-100k-15-m6": ("correlated_q", 100_000, 15, 6, 42)}
+
+
 def write_digest(name, threads):
     """Per-cuboid digest of the reference's own STSC on one full-size
-    workload: for every computed cuboid its skyline and extended-skyline
-    counts and the 64-bit hashes of both ascending id lists, plus a hash of
-    the generated points (so a generator that differs is reported as such)."""
-    kind, n, d, max_d, seed = datagen.CONFIGS[name]
+    workload (or a SCALED stand-in): for every computed cuboid its skyline
+    and extended-skyline counts and the 64-bit hashes of both ascending id
+    lists, plus a hash of the generated points (so a generator that differs
+    is reported as such)."""
+    kind, n, d, max_d, seed = SCALED[name] if name in SCALED else datagen.CONFIGS[name]
     x = datagen.generate(kind, n, d, seed)
     t0 = time.time()
     res = oracle.ref_stsc(x, max_d, threads=threads)

@@ -74,7 +74,8 @@ def test_full_space_always_present_under_cap(gpu_ctx):
         assert len(r.cuboid(0b111)) == 0
 
 
-DIGESTS = ["uniform-100k-6", "anticorr-1m-10", "ties-581k-10", "corrq-566k-15-m6"]
+DIGESTS = ["uniform-100k-6", "anticorr-1m-10", "ties-581k-10", "corrq-566k-15-m6",
+           "corrq-100k-15-m6"]
 
 
 @pytest.mark.parametrize("form", ["mdmc/batched", "sdsc/batched", "sdsc/plain"])
@@ -83,7 +84,7 @@ def test_full_size_digest(gpu_ctx, name, form):
     dg = load_digest(name)
     if dg is None:
         pytest.skip(f"no reference digest for {name}")
-    kind, n, d, m, seed = datagen.CONFIGS[name]
+    kind, n, d, m, seed = str(dg["kind"]), int(dg["n"]), int(dg["d"]), int(dg["max_d"]), int(dg["seed"])
     x = datagen.generate(kind, n, d, seed)
     assert points_hash(x) == int(dg["points_hash"]), "the generator gives other points than the digest's"
     algo, mode = form.split("/")
