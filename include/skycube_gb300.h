@@ -130,6 +130,17 @@ int skc_dataset_free(skc_dataset* ds);
 int skc_skycube(skc_context* ctx, skc_dataset* ds, const skc_options* opt,
                 skc_result** out);
 
+/* Skycubes of `count` resident datasets in one call; results[i] equals
+ * skc_skycube(ctx, datasets[i], &opts[i]) (opts NULL: defaults). Every
+ * dataset's full-space step runs first; then ONE persistent lattice launch
+ * (SKC_FORM_LEVELS) carries the cuboids of all the datasets whose skycube
+ * takes that form, and the other datasets take their own launches. The
+ * serving loop batches waiting requests through it. No reference
+ * counterpart (the suite computes one dataset per run). On error no result
+ * is returned. */
+int skc_skycube_batch(skc_context* ctx, skc_dataset* const* datasets,
+                      const skc_options* opts, int count, skc_result** results);
+
 /* Number of attributes of the result's dataset and number of candidate
  * points (full-space skyline plus extended skyline). */
 /* Which computation produced the result (SKC_FORM_*), and for
@@ -173,11 +184,15 @@ int skc_result_bitmaps(skc_result* res, const uint32_t** bits,
 int skc_result_free(skc_result* res);
 
 /* ---- Serving loop (continuous batching) ---------------------------------
- * A server owns `slots` worker threads, each with its own CUDA stream.
- * Submitted requests wait in FIFO order; the first one starts as soon as a
- * slot is free and its estimated device-memory footprint fits what the
+ * A server owns `slots` worker threads, each with a high- and a
+ * low-priority CUDA stream (requests with n * 2^d >= 2^29 take the low
+ * one). Submitted requests wait in FIFO order; the first one starts as soon
+ * as a slot is free and its estimated device-memory footprint fits what the
  * requests in flight leave of `budget` (bytes; 0: 80% of the free device
- * memory). Requests whose estimate exceeds the whole budget are rejected
+ * memory). A capped skycube request (batched form, max_d <= 4 and <= d - 2,
+ * no bitmaps) takes the capped skycube requests right behind it in the
+ * queue (up to 8, within the budget) into the same pass: one persistent
+ * lattice launch for all of them (skc_skycube_batch). Requests whose estimate exceeds the whole budget are rejected
  * with SKC_ERR_REJECTED at submission. Requests that run at the same time
  * overlap on the device. Results come back in host memory (their device
  * views are empty). Host rows passed to skc_server_submit must stay valid
@@ -206,6 +221,12 @@ int skc_server_wait(skc_server* srv, uint64_t ticket, skc_result** out,
                     skc_server_timing* timing);
 int skc_server_stats(skc_server* srv, uint64_t* admitted,
                      uint64_t* peak_in_flight, uint64_t* budget);
+/* Batches the server ran (groups of requests that shared one lattice
+ * launch: batched capped skycubes, SKC_FORM_LEVELS candidates, taken
+ * together from the head of the queue when they arrive while the slots are
+ * busy), requests served in them, and the largest batch. */
+int skc_server_batch_stats(skc_server* srv, uint64_t* batches,
+                           uint64_t* batched_requests, uint64_t* largest);
 /* Waits for queued and running requests, then stops the workers. */
 int skc_server_destroy(skc_server* srv);
 

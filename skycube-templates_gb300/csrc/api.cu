@@ -1664,6 +1664,127 @@ static int skycube_exec(Exec& E, skc_dataset* ds, const skc_options* opt, skc_re
   return SKC_OK;
 }
 
+// Several skycubes in one pass: every dataset's full-space step, then ONE
+// lattice launch shared by all the datasets whose skycube takes the lattice
+// form, the other forms dataset by dataset. results[i] equals what
+// skycube_exec gives for dataset i alone.
+static int skycube_exec_batch(Exec& E, const std::vector<skc_dataset*>& dss,
+                              const std::vector<skc_options>& opts,
+                              std::vector<skc_result*>* out) {
+  skc_context* ctx = E.ctx;
+  const size_t nb = dss.size();
+  out->assign(nb, nullptr);
+  SKC_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = E.stream;
+  std::vector<skc_options> o(nb);
+  std::vector<int> max_d(nb);
+  std::vector<RunParams> P(nb);
+  for (size_t i = 0; i < nb; ++i) {
+    SKC_TRY(check_options(dss[i], &opts[i], &o[i]));
+    const int d = dss[i]->d;
+    max_d[i] = (o[i].max_d <= 0 || o[i].max_d > d) ? d : o[i].max_d;
+    SKC_TRY(resolve_params(dss[i], s, o[i], max_d[i], &P[i]));
+  }
+  std::vector<skc_result*> R(nb, nullptr);
+  for (size_t i = 0; i < nb; ++i) {
+    R[i] = new skc_result;
+    R[i]->ctx = ctx;
+    R[i]->stream = s;
+    R[i]->d = dss[i]->d;
+    R[i]->max_d = o[i].subspace ? __builtin_popcount(o[i].subspace) : max_d[i];
+    R[i]->algo = o[i].algo;
+  }
+  int st = SKC_OK;
+  {
+    Arena A(s);
+    Tracer T(E);
+    std::vector<FullSpace> F(nb);  // referenced by the lattice jobs: no reallocation
+    std::vector<LatticeJob> jobs;
+    std::vector<size_t> job_of;
+    for (size_t i = 0; i < nb && st == SKC_OK; ++i) {
+      skc_dataset* ds = dss[i];
+      st = run_full_space(E, ds, P[i], A, F[i], T);
+      if (st != SKC_OK) break;
+      R[i]->n_cand = F[i].h_counts[2];
+      if (o[i].subspace) {
+        R[i]->form = SKC_FORM_SKYLINE;
+        st = run_single_cuboid(E, ds, o[i].subspace, P[i], A, F[i], R[i], T);
+      } else if (o[i].algo == SKC_ALGO_SDSC && o[i].mode == SKC_MODE_PLAIN) {
+        R[i]->form = SKC_FORM_CUBOIDS;
+        st = run_sdsc_plain(E, ds, max_d[i], P[i].depth, A, F[i], R[i], T);
+      } else if (use_levels(E, ds, o[i], max_d[i], F[i])) {
+        LatticeJob J;
+        J.ds = ds;
+        J.max_d = max_d[i];
+        J.depth = P[i].depth;
+        J.want_ext = o[i].want_extended || o[i].algo == SKC_ALGO_SDSC;
+        J.F = &F[i];
+        J.R = R[i];
+        jobs.push_back(std::move(J));
+        job_of.push_back(i);
+      } else {
+        R[i]->form = SKC_FORM_BITMAPS;
+        st = run_bitmaps(E, ds, o[i], P[i], max_d[i], A, F[i], R[i], T);
+      }
+    }
+    if (st == SKC_OK && !jobs.empty()) {
+      st = run_lattice(E, jobs, A, T);
+      for (size_t k = 0; k < jobs.size() && st == SKC_OK; ++k) {
+        const size_t i = job_of[k];
+        R[i]->form = SKC_FORM_LEVELS;
+        if (jobs[k].status == kLvGiveUp) {
+          R[i]->form = SKC_FORM_BITMAPS;
+          st = run_bitmaps(E, dss[i], o[i], P[i], max_d[i], A, F[i], R[i], T);
+        }
+      }
+    }
+    T.mark("end");
+  }
+  if (st == SKC_OK) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = set_error(SKC_ERR_CUDA, "skycube batch failed: %s", cudaGetErrorString(e));
+  }
+  if (st != SKC_OK) {
+    std::string msg = g_err;
+    for (auto* r : R) skc_result_free(r);
+    g_err = msg;
+    return st;
+  }
+  {
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    for (auto* r : R) ctx->results.insert(r);
+  }
+  *out = R;
+  return SKC_OK;
+}
+
+int skc_skycube_batch(skc_context* ctx, skc_dataset* const* datasets, const skc_options* opts,
+                      int count, skc_result** results) {
+  clear_error();
+  if (!ctx || !datasets || !results || count < 0) return set_error(SKC_ERR_INVALID, "NULL argument");
+  std::vector<skc_dataset*> dss(count);
+  std::vector<skc_options> o(count);
+  for (int i = 0; i < count; ++i) {
+    results[i] = nullptr;
+    if (!datasets[i]) return set_error(SKC_ERR_INVALID, "dataset %d is NULL", i);
+    if (datasets[i]->ctx != ctx)
+      return set_error(SKC_ERR_INVALID, "dataset %d belongs to another (or a destroyed) context", i);
+    dss[i] = datasets[i];
+    if (opts) o[i] = opts[i];
+    else skc_options_init(&o[i]);
+  }
+  Exec E;
+  E.ctx = ctx;
+  E.stream = ctx->stream;
+  std::vector<skc_result*> R;
+  const int st = skycube_exec_batch(E, dss, o, &R);
+  ctx->phases = E.phases;
+  ctx->last_ms = E.ms;
+  if (st == SKC_OK)
+    for (int i = 0; i < count; ++i) results[i] = R[i];
+  return st;
+}
+
 int skc_skycube(skc_context* ctx, skc_dataset* ds, const skc_options* opt, skc_result** out) {
   clear_error();
   if (!ctx || !ds || !out) return set_error(SKC_ERR_INVALID, "NULL argument");
@@ -2265,7 +2386,18 @@ struct skc_server {
   bool stopping = false;
   uint64_t next_ticket = 1;
   uint64_t admitted = 0, peak_in_flight = 0, in_flight = 0;
+  uint64_t batches = 0, batched_requests = 0, largest_batch = 0;
 };
+
+// Requests that may share one lattice launch: batched capped skycubes the
+// lattice form may take (max_d <= kLvMaxDims and <= d - 2, no bitmaps).
+static bool batchable(const Request& q) {
+  const skc_options& o = q.opt;
+  const int md = (o.max_d <= 0 || o.max_d > q.d) ? q.d : o.max_d;
+  return !o.subspace && o.mode == SKC_MODE_BATCHED && !o.want_bitmaps &&
+         o.form != SKC_FORM_BITMAPS && md <= kLvMaxDims && md <= q.d - 2;
+}
+constexpr size_t kMaxServerBatch = 8;
 
 // Estimated device memory of one request: the resident points, the full-space
 // pipeline, and the bitmap or per-cuboid stage with every point a candidate
@@ -2344,10 +2476,55 @@ static void serve_one(skc_server* S, cudaStream_t stream, Request& q) {
   }
 }
 
+// Several batchable requests in one pass (skycube_exec_batch): their
+// uploads, one lattice launch for all, their copies out.
+static void serve_batch(skc_server* S, cudaStream_t stream,
+                        std::vector<std::shared_ptr<Request>>& qs) {
+  clear_error();
+  Exec E;
+  E.ctx = S->ctx;
+  E.stream = stream;
+  const size_t nb = qs.size();
+  std::vector<skc_dataset*> dss(nb, nullptr);
+  std::vector<skc_options> opts(nb);
+  std::vector<bool> own(nb, false);
+  int st = SKC_OK;
+  for (size_t i = 0; i < nb && st == SKC_OK; ++i) {
+    Request& q = *qs[i];
+    opts[i] = q.opt;
+    if (q.ds) {
+      dss[i] = q.ds;
+    } else {
+      st = upload_on(S->ctx, stream, q.rows, q.n, q.d, true, &dss[i]);
+      own[i] = st == SKC_OK;
+    }
+  }
+  std::vector<skc_result*> R;
+  if (st == SKC_OK) st = skycube_exec_batch(E, dss, opts, &R);
+  for (size_t i = 0; i < nb; ++i) {
+    Request& q = *qs[i];
+    q.device_ms = E.ms;
+    q.status = st;
+    if (st == SKC_OK) {
+      q.result = R[i];
+      q.status = result_to_host(q.result);
+    }
+    if (q.status != SKC_OK) {
+      q.err = g_err;
+      if (q.result) {
+        skc_result_free(q.result);
+        q.result = nullptr;
+      }
+    }
+    if (own[i] && dss[i]) skc_dataset_free(dss[i]);
+  }
+}
+
 static void worker_loop(skc_server* S, int slot) {
   cudaSetDevice(S->ctx->device);
   for (;;) {
-    std::shared_ptr<Request> q;
+    std::vector<std::shared_ptr<Request>> batch;
+    bool heavy = false;
     {
       std::unique_lock<std::mutex> lk(S->mu);
       S->cv_work.wait(lk, [&] {
@@ -2355,21 +2532,40 @@ static void worker_loop(skc_server* S, int slot) {
                                S->queue.front()->footprint <= S->budget - S->in_use);
       });
       if (S->stopping) return;
-      q = S->queue.front();
-      S->queue.pop_front();
-      S->in_use += q->footprint;
-      ++S->admitted;
-      ++S->in_flight;
+      // The head of the queue, and when it is a batchable request the
+      // batchable requests right behind it that fit the budget.
+      const auto now = std::chrono::steady_clock::now();
+      do {
+        auto q = S->queue.front();
+        S->queue.pop_front();
+        S->in_use += q->footprint;
+        ++S->admitted;
+        ++S->in_flight;
+        q->t_start = now;
+        heavy = heavy || q->heavy;
+        batch.push_back(q);
+      } while (batchable(*batch[0]) && batch.size() < kMaxServerBatch && !S->queue.empty() &&
+               batchable(*S->queue.front()) &&
+               S->queue.front()->footprint <= S->budget - S->in_use);
       S->peak_in_flight = std::max(S->peak_in_flight, S->in_flight);
-      q->t_start = std::chrono::steady_clock::now();
+      if (batch.size() > 1) {
+        ++S->batches;
+        S->batched_requests += batch.size();
+        S->largest_batch = std::max<uint64_t>(S->largest_batch, batch.size());
+      }
     }
-    serve_one(S, q->heavy ? S->streams_lo[slot] : S->streams[slot], *q);
+    cudaStream_t stream = heavy ? S->streams_lo[slot] : S->streams[slot];
+    if (batch.size() == 1) serve_one(S, stream, *batch[0]);
+    else serve_batch(S, stream, batch);
     {
       std::lock_guard<std::mutex> lk(S->mu);
-      S->in_use -= q->footprint;
-      --S->in_flight;
-      q->t_end = std::chrono::steady_clock::now();
-      q->done = true;
+      const auto now = std::chrono::steady_clock::now();
+      for (auto& q : batch) {
+        S->in_use -= q->footprint;
+        --S->in_flight;
+        q->t_end = now;
+        q->done = true;
+      }
     }
     S->cv_done.notify_all();
     S->cv_work.notify_all();
@@ -2508,6 +2704,17 @@ int skc_server_stats(skc_server* S, uint64_t* admitted, uint64_t* peak_in_flight
   if (admitted) *admitted = S->admitted;
   if (peak_in_flight) *peak_in_flight = S->peak_in_flight;
   if (budget) *budget = S->budget;
+  return SKC_OK;
+}
+
+int skc_server_batch_stats(skc_server* S, uint64_t* batches, uint64_t* batched_requests,
+                           uint64_t* largest) {
+  clear_error();
+  if (!S) return set_error(SKC_ERR_INVALID, "NULL server");
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (batches) *batches = S->batches;
+  if (batched_requests) *batched_requests = S->batched_requests;
+  if (largest) *largest = S->largest_batch;
   return SKC_OK;
 }
 

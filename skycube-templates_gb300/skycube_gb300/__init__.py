@@ -72,6 +72,8 @@ def lib():
         "skc_dataset_upload_device": (i32, [vp, vp, u64, i32, P(vp)]),
         "skc_dataset_free": (i32, [vp]),
         "skc_skycube": (i32, [vp, vp, P(_Options), P(vp)]),
+        "skc_skycube_batch": (i32, [vp, P(vp), P(_Options), i32, P(vp)]),
+        "skc_server_batch_stats": (i32, [vp, P(u64), P(u64), P(u64)]),
         "skc_result_info": (i32, [vp, P(i32), P(u64), P(u64)]),
         "skc_result_form": (i32, [vp, P(i32), P(i32)]),
         "skc_result_cuboid": (i32, [vp, u32, P(P(u32)), P(u64)]),
@@ -317,6 +319,23 @@ def skycube(ctx, ds, algo="mdmc", mode="batched", max_d=0, depth=0,
     return Result(ctx, h, ds.d, md)
 
 
+def skycube_batch(ctx, datasets, opts_list):
+    """skc_skycube_batch: the skycubes of several resident datasets in one
+    pass (one lattice launch shared by those that take the level form).
+    opts_list holds one dict of skycube() keyword options per dataset."""
+    n = len(datasets)
+    arr = (ctypes.c_void_p * n)(*[ds.handle.value for ds in datasets])
+    opts = (_Options * n)(*[options(**o) for o in opts_list])
+    outs = (ctypes.c_void_p * n)()
+    _check(lib().skc_skycube_batch(ctx.handle, arr, opts, n, outs))
+    res = []
+    for ds, o, h in zip(datasets, opts_list, outs):
+        md = o.get("max_d", 0)
+        md = ds.d if md <= 0 or md > ds.d else md
+        res.append(Result(ctx, ctypes.c_void_p(h), ds.d, md))
+    return res
+
+
 class Plan:
     """skc_plan_*: the batched skycube of one dataset captured as a CUDA
     graph; execute() replays it on the dataset's current points."""
@@ -408,6 +427,12 @@ class Server:
         a, p, b = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
         _check(lib().skc_server_stats(self.handle, ctypes.byref(a), ctypes.byref(p), ctypes.byref(b)))
         return {"admitted": a.value, "peak_in_flight": p.value, "budget": b.value}
+
+    def batch_stats(self):
+        b, r, m = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib().skc_server_batch_stats(self.handle, ctypes.byref(b), ctypes.byref(r),
+                                            ctypes.byref(m)))
+        return {"batches": b.value, "batched_requests": r.value, "largest": m.value}
 
     def close(self):
         if self.handle:

@@ -1,6 +1,7 @@
-"""The level form of capped skycubes (max_d <= 4): every cuboid of a lattice
-level in one filter and one sort-filter launch, from its smallest computed
-parent. Checked against the C oracle on seeded inputs (the form forced,
+"""The level form of capped skycubes (max_d <= 4): every wanted cuboid in
+one persistent lattice launch whose device queue runs the levels top down,
+each cuboid from its smallest computed parent; several datasets share one
+launch through skc_skycube_batch. Checked against the C oracle on seeded inputs (the form forced,
 each case asserting that it ran), on a tie-heavy input whose one-attribute skylines
 exceed the kernel's window (so the per-cuboid fallback runs), and against
 the bitmap form at sizes the oracle would take minutes on. Exact id-set
@@ -109,3 +110,47 @@ def test_levels_equal_bitmap_form(gpu_ctx, kind, n, d, max_d, seed):
     a.close()
     b.close()
     ds.close()
+
+
+def test_batch_of_datasets_equals_each_alone(gpu_ctx):
+    """skc_skycube_batch: three capped skycubes in one lattice launch (one of
+    them tie-heavy enough to use the per-cuboid fallback), a full skycube in
+    the bitmap form and a skyline query, each equal to its own skc_skycube
+    and the capped ones to the oracle."""
+    rng = np.random.default_rng(9)
+    cases = [
+        (datagen.generate("anticorrelated", 9000, 7, 21), dict(max_d=3, want_extended=True)),
+        (datagen.generate("uniform", 15000, 12, 22), dict(algo="sdsc", max_d=4, want_extended=True)),
+        (np.floor(rng.random((8000, 6)) * 3).astype(np.float32), dict(max_d=2, want_extended=True)),
+        (datagen.generate("correlated", 20000, 8, 23), dict(want_extended=True)),
+        (datagen.generate("ties", 10000, 9, 24), dict(subspace=0b101100111, want_extended=True)),
+    ]
+    dss = [sk.Dataset(gpu_ctx, x) for x, _ in cases]
+    for o in (dict(form="levels"), {}):
+        opts = [{**o, **c} if c.get("max_d", 99) <= 4 else c for _, c in cases]
+        batch = sk.skycube_batch(gpu_ctx, dss, opts)
+        forms = [r.form()[0] for r in batch]
+        if o:
+            assert forms[:3] == ["levels"] * 3, forms
+        for (x, c), ds, o2, rb in zip(cases, dss, opts, batch):
+            ra = sk.skycube(gpu_ctx, ds, **o2)
+            d = x.shape[1]
+            md = c.get("max_d", 0) or d
+            if c.get("subspace"):
+                S = c["subspace"]
+                assert np.array_equal(rb.cuboid(S), ra.cuboid(S))
+                assert np.array_equal(rb.extended(S), ra.extended(S))
+            else:
+                for cub in range(1, 1 << d):
+                    if bin(cub).count("1") <= md or cub == (1 << d) - 1:
+                        assert np.array_equal(rb.cuboid(cub), ra.cuboid(cub)), (c, cub)
+                        assert np.array_equal(rb.extended(cub), ra.extended(cub)), (c, cub)
+            ra.close()
+        for (x, c), rb in zip(cases[:3], batch[:3]):
+            sky, ext = oracle.stsc(x, c["max_d"])
+            for cub in sky:
+                assert np.array_equal(rb.cuboid(cub), sky[cub]) and np.array_equal(rb.extended(cub), ext[cub])
+        for r in batch:
+            r.close()
+    for ds in dss:
+        ds.close()

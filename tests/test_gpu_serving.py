@@ -129,3 +129,33 @@ def test_one_waiter_per_ticket(gpu_ctx):
     h = ctypes.c_void_p()
     assert L.skc_server_wait(srv.handle, ctypes.c_uint64(t), ctypes.byref(h), None) == 1
     srv.close()
+
+
+def test_capped_skycubes_batched_into_one_launch(gpu_ctx):
+    """With one slot, capped skycube requests that wait behind a running
+    request are taken together into one lattice launch; each result equals
+    the request served alone."""
+    xs = [datagen.generate(k, 30000, 10, 200 + i) for i, k in
+          enumerate(("anticorrelated", "uniform", "correlated", "anticorrelated", "uniform"))]
+    opts = dict(max_d=3, want_extended=True, form="levels")
+    alone = []
+    for x in xs:
+        ds = sk.Dataset(gpu_ctx, x)
+        r = sk.skycube(gpu_ctx, ds, **opts)
+        alone.append(snapshot(r, True))
+        r.close()
+        ds.close()
+    srv = sk.Server(gpu_ctx, slots=1)
+    big = srv.submit(datagen.generate("anticorrelated", 300000, 10, 7))  # keeps the slot busy
+    ts = [srv.submit(x, **opts) for x in xs]
+    srv.wait(big)[0].close()
+    for t, want in zip(ts, alone):
+        r, _ = srv.wait(t)
+        got = snapshot(r, True)
+        assert got.keys() == want.keys()
+        for c in got:
+            assert np.array_equal(got[c], want[c]), c
+        r.close()
+    st = srv.batch_stats()
+    assert st["batches"] >= 1 and st["largest"] >= 2, st
+    srv.close()
