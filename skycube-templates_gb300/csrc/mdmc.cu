@@ -822,15 +822,15 @@ __global__ void __launch_bounds__(256) k_bits_count(
       const uint32_t v = counted_bits(bits, W, row0 + s * 32 + lane, m, w, count_set) & wanted;
       if (dense) {
 #pragma unroll
-        for (int b = 0; b < 32; ++b) {
-          const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
-          if (lane == b) cnt += __popc(bal);
+        for (int b = 0; b < 32; ++b) {  // one warp reduction per bit column
+          const uint32_t tot = __reduce_add_sync(kFull, (v >> b) & 1u);
+          if (lane == b) cnt += tot;
         }
       } else {
         for (uint32_t mm = wanted; mm; mm &= mm - 1) {
           const int b = __ffs(mm) - 1;
-          const uint32_t bal = __ballot_sync(kFull, (v >> b) & 1u);
-          if (lane == b) cnt += __popc(bal);
+          const uint32_t tot = __reduce_add_sync(kFull, (v >> b) & 1u);
+          if (lane == b) cnt += tot;
         }
       }
     }
