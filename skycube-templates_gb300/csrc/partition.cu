@@ -243,8 +243,12 @@ __global__ void __launch_bounds__(1024) k_split_plan(const uint32_t* __restrict_
 // sorted partition at the first q above its own strength level.
 constexpr uint32_t kFullMask = 0xffffffffu;
 
+// Up to 10 attributes the sliced variant holds 6 CTAs per SM (40 registers,
+// no spill; it had taken 48 and 5 CTAs): 1M x 10 anticorrelated full
+// skycube 28.4 -> 27.7 ms. Above 10 attributes the bound would spill, and
+// the unsliced level-cutoff variant (LV) keeps the free register budget.
 template <int NA, bool LV>
-__global__ void __launch_bounds__(256) k_skyline_part(PartKernelArgs a) {
+__global__ void __launch_bounds__(256, (!LV && NA <= 10) ? 6 : 1) k_skyline_part(PartKernelArgs a) {
   constexpr int NW = (NA + 3) / 4;
   constexpr int TQ = 256;
   __shared__ uint4 q_cells[TQ];
