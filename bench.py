@@ -71,6 +71,10 @@ def parse_args():
                          "dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum "
                          "-k regex:k_bitmaps over this benchmark, with the sha256 of the bitmap "
                          "kernel's sources, then exit")
+    ap.add_argument("--record-useful", action="store_true",
+                    help="build the bitmap kernel's counters library, run the workload once with "
+                         "it and add its per-candidate work figures to "
+                         "profiles/kernel_counters_<workload>.json, then exit")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the other benchmark configurations (100k x 6, ties, 15-d capped)")
     return ap.parse_args()
@@ -788,8 +792,54 @@ def record_counters(csv_path, workload):
     print(json.dumps(out))
 
 
+def record_useful(workload):
+    """Per-candidate work of the bitmap kernel from its counters build (the
+    same sources with SKC_BITMAP_COUNTERS=1), into the counts file."""
+    import ctypes
+    import importlib
+    bmod = importlib.import_module("skycube_gb300.build")
+    path = bmod.build(counters=True)
+    import skycube_gb300 as sk
+    sk.LIB_PATH = path
+    L = sk.lib()
+    f = L.skc_debug_bitmap_counters
+    f.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    f.restype = ctypes.c_int
+    kind, n, d, max_d, seed = datagen.CONFIGS[workload]
+    ctx = sk.Context(0)
+    ds = sk.Dataset(ctx, datagen.generate(kind, n, d, seed))
+    sk.skycube(ctx, ds, "mdmc", "batched", max_d=max_d).close()
+    c = (ctypes.c_ulonglong * 16)()
+    f(c, 1)
+    sk.skycube(ctx, ds, "mdmc", "batched", max_d=max_d).close()
+    f(c, 0)
+    m = max(1, c[0])
+    names = ["candidates", "partition_ballots", "partitions_visited", "box_test_steps",
+             "block_boxes_tested", "blocks_walked", "walked_blocks_all_covered",
+             "strict_updates", "tie_pairs", "uncovered_q_tested"]
+    useful = {"per_candidate": {nm: round(c[i] / m, 3) for i, nm in enumerate(names) if i},
+              "candidates": int(c[0]),
+              "useful_block_fraction": round(1 - c[6] / max(1, c[5]), 4),
+              "note": "counters build of the same sources (SKC_BITMAP_COUNTERS=1): a walked "
+                      "block is useful when at least one of its 32 q's was not already "
+                      "covered by STRICT"}
+    cpath = os.path.join(REPO, "profiles", f"kernel_counters_{workload}.json")
+    with open(cpath) as fh:
+        t = json.load(fh)
+    kb = t.setdefault("k_bitmaps", {})
+    if kb.get("sources_sha256") != bitmap_sources_sha():
+        raise SystemExit("the recorded instruction count is for other sources: record it first")
+    kb["useful"] = useful
+    with open(cpath, "w") as fh:
+        json.dump(t, fh, indent=1)
+    print(json.dumps(useful))
+
+
 def main():
     args = parse_args()
+    if args.record_useful:
+        record_useful(args.workload)
+        return
     if args.record_counters:
         record_counters(args.record_counters, args.workload)
         return

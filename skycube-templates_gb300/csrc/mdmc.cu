@@ -31,6 +31,10 @@
 // L >> 5, else empty.
 #include "kernels.cuh"
 
+#ifndef SKC_BITMAP_COUNTERS
+#define SKC_BITMAP_COUNTERS 0
+#endif
+
 namespace skc {
 
 // c_submask[x] = bit b set iff b is a subset of x (5-bit masks).
@@ -58,6 +62,20 @@ void upload_submask_table() {
 }
 
 constexpr uint32_t kFull = 0xffffffffu;
+
+// Work counters of the bitmap kernel, compiled only into the counters build
+// (SKC_BITMAP_COUNTERS=1, skycube_gb300.build(counters=True)); the normal
+// build has none of this code. Per launch, summed over candidates:
+// [0] candidates, [1] partition ballots, [2] partitions visited, [3] box-test
+// steps, [4] block boxes tested, [5] blocks walked, [6] walked blocks whose
+// q's were all covered already, [7] STRICT updates, [8] tie pairs,
+// [9] q's tested that were not covered.
+#if SKC_BITMAP_COUNTERS
+__device__ unsigned long long g_bitmap_counters[16];
+#define SKC_COUNT(i, v) (cnt_[i] += (v))
+#else
+#define SKC_COUNT(i, v) ((void)0)
+#endif
 
 template <int D>
 struct BitState {
@@ -356,12 +374,21 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
   // about as much as walking W / 32 blocks).
   constexpr uint32_t kCloseBlocks = W / 32;
 
+#if SKC_BITMAP_COUNTERS
+  unsigned long long cnt_[10] = {};
+#endif
   for (;;) {
     // The warp takes `chunk` consecutive candidates per grab.
     uint32_t p0 = 0;
     if (lane == 0) p0 = atomicAdd(work, chunk);
     p0 = __shfl_sync(kFull, p0, 0);
-    if (p0 >= pend) break;
+    if (p0 >= pend) {
+#if SKC_BITMAP_COUNTERS
+      if (lane == 0)
+        for (int i = 0; i < 10; ++i) atomicAdd(&g_bitmap_counters[i], cnt_[i]);
+#endif
+      break;
+    }
     const uint32_t p1 = min(pend, p0 + chunk);
     for (uint32_t p = p0; p < p1; ++p) {
     const uint4 pc4 = pcells[p];
@@ -379,6 +406,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
 
     // STRICT starts with the empty subspace so that q's worse on every
     // attribute (U == 0) test as "nothing new".
+    SKC_COUNT(0, 1);
     uint32_t sat = 0;
     if (REG) {
       sat = (wi == 0) ? 1u : 0u;
@@ -425,7 +453,11 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
         U |= pack_guards(ge_bytes(pH[w], word_of(q4, w))) << (4 * w);
       U &= NSUB - 1;
       const bool hit = in_strict(U);
-      if (__all_sync(kFull, hit)) return;
+      if (__all_sync(kFull, hit)) {
+        SKC_COUNT(6, 1);
+        return;
+      }
+      SKC_COUNT(9, __popc(__ballot_sync(kFull, !hit)));
 
       uint32_t le = 0, lt = 0;
       if (!hit) {
@@ -456,6 +488,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
       // inside STRICT changes nothing.
       const bool tie_lane = !hit && le != lt && !t_le;
       const uint32_t tb = __ballot_sync(kFull, tie_lane);
+      SKC_COUNT(8, __popc(tb));
       if (tb) {
         if constexpr (BS::A_SMEM) {
           if (!touched) {
@@ -495,6 +528,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
         todo &= todo - 1;
         const uint32_t L = __shfl_sync(kFull, lt, src);
         if (in_strict(L)) continue;  // covered by an earlier update
+        SKC_COUNT(7, 1);
         if constexpr (CAP) dirty = true;
         if (REG) {
           if ((wi & ~(L >> 5)) == 0) sat |= c_submask[L & 31];
@@ -543,6 +577,8 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
       const bool sb_strict = in_strict(Sb);
       const bool sel = (qbeg_l != qend_l) && !sb_strict;
       const uint32_t parts = __ballot_sync(kFull, sel);
+      SKC_COUNT(1, 1);
+      SKC_COUNT(2, __popc(parts));
       if (!parts) continue;
       // The blocks of all selected partitions form one list, so their box
       // tests fill the 32 lanes: lane t's partition owns blocks [bf, be).
@@ -589,6 +625,9 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
         }
         const bool ub_strict = in_strict(Ub);  // every lane (shuffle)
         uint32_t blocks = __ballot_sync(kFull, in_list && !ub_strict);
+        SKC_COUNT(3, 1);
+        SKC_COUNT(4, min(32u, total - t0));
+        SKC_COUNT(5, __popc(blocks));
         if constexpr (CAP && !REG) since += 1 + __popc(blocks);
         while (blocks) {
           const int bs = __ffs(blocks) - 1;
@@ -752,6 +791,20 @@ static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
     case 16: return fn<16>(__VA_ARGS__);                \
     default: return set_error(SKC_ERR_INVALID, "unsupported d=%d", d); \
   }
+
+#if SKC_BITMAP_COUNTERS
+// Counters build only: copies the summed counters out and, when reset is
+// nonzero, zeroes them.
+extern "C" int skc_debug_bitmap_counters(unsigned long long* out, int reset) {
+  if (cudaMemcpyFromSymbol(out, g_bitmap_counters, sizeof(g_bitmap_counters)) != cudaSuccess)
+    return SKC_ERR_CUDA;
+  if (reset) {
+    unsigned long long z[16] = {};
+    if (cudaMemcpyToSymbol(g_bitmap_counters, z, sizeof(z)) != cudaSuccess) return SKC_ERR_CUDA;
+  }
+  return SKC_OK;
+}
+#endif
 
 int launch_bitmaps(cudaStream_t s, int d, int num_sms, const BitmapArgs& a) {
   SKC_BITMAP_DISPATCH(launch_bitmaps_d, s, num_sms, a)

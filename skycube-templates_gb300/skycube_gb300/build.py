@@ -19,6 +19,11 @@ INCLUDE = os.path.join(REPO_ROOT, "include")
 BUILD = os.path.join(PKG_ROOT, "_build")
 LIB_NAME = "libskycube_gb300.so"
 LIB_PATH = os.path.join(BUILD, LIB_NAME)
+# The counters build: the same library with the bitmap kernel's work
+# counters compiled in (SKC_BITMAP_COUNTERS=1, skc_debug_bitmap_counters);
+# used to measure the kernel's useful work, never by the product.
+BUILD_COUNTERS = os.path.join(PKG_ROOT, "_build_counters")
+COUNTERS_LIB_PATH = os.path.join(BUILD_COUNTERS, LIB_NAME)
 CLI_PATH = os.path.join(BUILD, "skycube")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -51,9 +56,12 @@ def _stale(target, sources):
     return any(os.path.getmtime(s) > t for s in sources)
 
 
-def build(verbose=False, force=False, ptxas_verbose=False):
-    """Compiles the library and the CLI if any source is newer; returns LIB_PATH."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose=False, force=False, ptxas_verbose=False, counters=False):
+    """Compiles the library and the CLI if any source is newer; returns LIB_PATH.
+    counters=True builds the counters library instead (COUNTERS_LIB_PATH)."""
+    out_dir = BUILD_COUNTERS if counters else BUILD
+    lib_path = COUNTERS_LIB_PATH if counters else LIB_PATH
+    os.makedirs(out_dir, exist_ok=True)
     nvcc = _nvcc()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
     headers.append(os.path.join(INCLUDE, "skycube_gb300.h"))
@@ -61,18 +69,22 @@ def build(verbose=False, force=False, ptxas_verbose=False):
               "-I", INCLUDE, "-I", CSRC]
     if ptxas_verbose:
         common += ["-Xptxas", "-v"]
+    if counters:
+        common += ["-DSKC_BITMAP_COUNTERS=1"]
     objs, jobs = [], []
     for src in CU_SOURCES:
         path = os.path.join(CSRC, src)
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(out_dir, src.replace(".cu", ".o"))
         objs.append(obj)
         if force or _stale(obj, [path, *headers]):
             jobs.append([nvcc, *common, "-c", path, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for f in [ex.submit(_run, j, verbose) for j in jobs]:
             f.result()
-    if force or jobs or _stale(LIB_PATH, objs):
-        _run([nvcc, "-shared", *ARCH, "-o", LIB_PATH, *objs], verbose)
+    if force or jobs or _stale(lib_path, objs):
+        _run([nvcc, "-shared", *ARCH, "-o", lib_path, *objs], verbose)
+    if counters:
+        return lib_path
     cli_src = os.path.join(HOST, "cli.cpp")
     if os.path.exists(cli_src):
         host_headers = [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]
