@@ -851,6 +851,11 @@ static int run_lattice(Exec& E, std::vector<LatticeJob>& jobs, Arena& A, Tracer&
     }
   }
   const uint32_t n_items = (uint32_t)it_cub.size(), n_ph = (uint32_t)ph_size.size();
+  // Fault injection for the tests (SKC_FAULT_LATTICE_WAIT=1): the first
+  // phase counts one item more than exists, so the second phase's waits run
+  // out and the launch ends with SKC_ERR_TIMEOUT. Nothing faults or hangs.
+  if (const char* f = getenv("SKC_FAULT_LATTICE_WAIT"))
+    if (*f == '1' && n_ph > 1) ph_size[0] += 1;
 
   // 3. Device tables and scratch.
   LtArgs a{};

@@ -611,7 +611,7 @@ int launch_scatter_u4(cudaStream_t s, const uint4* in, const uint32_t* idx, cons
 // phase is done. Items are popped in order, so the items waited for are
 // running on resident CTAs (the launch is cooperative: every CTA is
 // resident); the waits are bounded and set status[0] when they run out.
-constexpr uint32_t kLtWaitLimit = 1u << 25;  // about 9 s of 256 ns sleeps
+constexpr uint32_t kLtWaitLimit = 1u << 23;  // about 2 s of 256 ns sleeps
 
 __device__ __forceinline__ bool lt_wait_phase(const uint32_t* done, uint32_t want,
                                               uint32_t* status) {

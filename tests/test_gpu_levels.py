@@ -154,3 +154,23 @@ def test_batch_of_datasets_equals_each_alone(gpu_ctx):
             r.close()
     for ds in dss:
         ds.close()
+
+
+def test_lattice_wait_runs_out_cleanly(gpu_ctx, monkeypatch):
+    """A lattice-phase wait that can never end (injected on the host: the
+    first phase counts one item more than exists) runs out after its bound
+    (about 2 s) and comes back as SKC_ERR_TIMEOUT; the context stays
+    usable."""
+    x = datagen.generate("uniform", 20000, 8, 31)
+    ds = sk.Dataset(gpu_ctx, x)
+    monkeypatch.setenv("SKC_FAULT_LATTICE_WAIT", "1")
+    with pytest.raises(sk.SkycubeError) as e:
+        sk.skycube(gpu_ctx, ds, max_d=3, form="levels")
+    assert e.value.code == 4 and "wait ran out" in str(e.value)
+    monkeypatch.delenv("SKC_FAULT_LATTICE_WAIT")
+    r = sk.skycube(gpu_ctx, ds, max_d=3, form="levels", want_extended=True)
+    sky, ext = oracle.stsc(x, 3)
+    for c in sky:
+        assert np.array_equal(r.cuboid(c), sky[c]) and np.array_equal(r.extended(c), ext[c])
+    r.close()
+    ds.close()
