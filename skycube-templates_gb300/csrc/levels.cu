@@ -415,11 +415,14 @@ __device__ uint32_t lv_sfs_cta(const CubAttrs& A, uint32_t c, uint32_t g,
           for (int a = 0; a < kLvMaxDims; ++a) wv[a] = w_v[a * kLvWin + j];
           r = lv_dom(w_c[j], wv, qpc, qpv, A);
         }
-        if (__ballot_sync(kWarpAll, r == 2)) {
+        // one warp OR of the statuses (r: 0 none, 1 dominates, 2 strictly):
+        // bit 1 some lane strictly dominates, bit 0 some lane dominates
+        const uint32_t any = __reduce_or_sync(kWarpAll, (uint32_t)r);
+        if (any & 2u) {
           st = 2;
           break;
         }
-        if (__ballot_sync(kWarpAll, r == 1)) st = 1;
+        if (any & 1u) st = 1;
       }
       if (lane == e) my_st = st;
     }
@@ -455,11 +458,14 @@ __device__ uint32_t lv_sfs_cta(const CubAttrs& A, uint32_t c, uint32_t g,
           for (int a = 0; a < kLvMaxDims; ++a) qv[a] = b_v[a * kLvThreads + q];
           r = lv_dom(b_c[q], qv, ppc, ppv, A);
         }
-        if (__ballot_sync(kWarpAll, r == 2)) {
+        // one warp OR of the statuses: bit 1 some lane strictly dominates,
+        // bit 0 some lane dominates
+        const uint32_t any = __reduce_or_sync(kWarpAll, (uint32_t)r);
+        if (any & 2u) {
           st = 2;
           break;
         }
-        if (__ballot_sync(kWarpAll, r == 1)) st = 1;
+        if (any & 1u) st = 1;
       }
       __syncwarp();
       if (lane == 0) b_st[p] = (uint8_t)st;  // only this warp reads b_st[p]
@@ -524,11 +530,12 @@ __device__ uint32_t lv_sfs_cta(const CubAttrs& A, uint32_t c, uint32_t g,
           r = lv_dom(pc, qv, pc, pv, A);
         }
       }
-      if (__ballot_sync(kWarpAll, r == 2)) {
+      const uint32_t any = __reduce_or_sync(kWarpAll, (uint32_t)r);
+      if (any & 2u) {
         st = 2;
         break;
       }
-      if (__ballot_sync(kWarpAll, r == 1)) st = 1;
+      if (any & 1u) st = 1;
     }
     if (lane == 0) {
       if (e < wn) w_st[e] = (uint8_t)st;
