@@ -223,7 +223,7 @@ int launch_bits_write(cudaStream_t s, const CompactArgs& a);
 constexpr int kLvMaxDims = 4;
 constexpr uint32_t kLvPruners = 32;    // per cuboid, from a strided sample
 constexpr uint32_t kLvSample = 1024;   // sampled list entries
-constexpr uint32_t kLvChunk = 4096;    // list entries per filter CTA
+constexpr uint32_t kLvChunk = 8192;    // list entries per filter item (staged in shared memory)
 constexpr uint32_t kLvThreads = 1024;  // sort-filter CTA, one batch per pass
 constexpr uint32_t kLvWin = 2048;      // skyline points per cuboid
 constexpr uint32_t kLvExt = 4096;      // extended-skyline points per cuboid
