@@ -736,7 +736,12 @@ static int run_sdsc_plain(Exec& E, skc_dataset* ds, int max_d,
 // smallest computed parent's skyline + extended skyline (or the full
 // space's candidates). Cuboids over the kernel's capacities are computed
 // afterwards with the single-cuboid pipeline.
-constexpr uint64_t kLvScratchBytes = 2048ull << 20;  // survivor scratch per launch
+// Survivor scratch per launch: at most this, and at most a quarter of the
+// free device memory. A level whose cuboids do not all fit is cut into
+// groups, each one more P/F/S phase triple; 8 GB holds the 1,820 cuboids
+// of a 16-d first level at cap 4 in one group (2 GB took three: 500k x 16
+// -m 4 53.1 -> 48.6 ms).
+constexpr uint64_t kLvScratchBytes = 8192ull << 20;
 constexpr uint32_t kLvMaxSurvivors = 262144;         // per cuboid
 // More cuboids over the capacities than this on a job's first level (heavy
 // exact ties: the per-cuboid fallback would dominate) and the bitmap form
@@ -811,7 +816,13 @@ static int run_lattice(Exec& E, std::vector<LatticeJob>& jobs, Arena& A, Tracer&
   int grid = 0;
   SKC_TRY(lattice_grid(ctx->num_sms, &grid));
   const uint32_t cap = (uint32_t)std::min<uint64_t>(max_cand, kLvMaxSurvivors);
-  const uint32_t G = (uint32_t)std::max<uint64_t>(1, kLvScratchBytes / ((uint64_t)cap * 10));
+  uint64_t scratch = kLvScratchBytes;
+  {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+      scratch = std::min<uint64_t>(scratch, std::max<uint64_t>(free_b / 4, 256ull << 20));
+  }
+  const uint32_t G = (uint32_t)std::max<uint64_t>(1, scratch / ((uint64_t)cap * 10));
   std::vector<uint32_t> c_scr(ncub, 0), it_cub, it_arg, it_phase, ph_size;
   std::vector<uint8_t> ph_kind;
   uint32_t g_used = 1;
