@@ -618,13 +618,26 @@ int launch_scatter_u4(cudaStream_t s, const uint4* in, const uint32_t* idx, cons
 // phase is done. Items are popped in order, so the items waited for are
 // running on resident CTAs (the launch is cooperative: every CTA is
 // resident); the waits are bounded and set status[0] when they run out.
+// After that no item runs: a skipped item still counts, so a later phase's
+// counter can fill up, and its items must not run on inputs the skipped
+// ones never wrote (a candidate-list pointer, a survivor count).
 constexpr uint32_t kLtWaitLimit = 1u << 23;  // about 2 s of 256 ns sleeps
 
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// True when the phase before is done and no wait has run out. The status is
+// read after the counter, both with acquire order: a skipped item set (or
+// saw) the status before its count, so a full counter that includes it
+// shows the status too.
 __device__ __forceinline__ bool lt_wait_phase(const uint32_t* done, uint32_t want,
                                               uint32_t* status) {
   for (uint32_t it = 0; it < kLtWaitLimit; ++it) {
-    if (ld_l2(done) >= want) return true;
-    if (ld_l2(status) != 0) return false;
+    if (ld_acquire(done) >= want) return ld_acquire(status) == 0;
+    if (ld_acquire(status) != 0) return false;
     __nanosleep(256);
   }
   atomicExch(status, 1u);
