@@ -815,14 +815,16 @@ def record_useful(workload):
     f(c, 0)
     m = max(1, c[0])
     names = ["candidates", "partition_ballots", "partitions_visited", "box_test_steps",
-             "block_boxes_tested", "blocks_walked", "walked_blocks_all_covered",
-             "strict_updates", "tie_pairs", "uncovered_q_tested"]
+             "block_boxes_tested", "walk_steps", "walk_steps_all_covered",
+             "strict_updates", "tie_pairs", "uncovered_q_tested", "sub_boxes_tested",
+             "sub_blocks_opened"]
     useful = {"per_candidate": {nm: round(c[i] / m, 3) for i, nm in enumerate(names) if i},
               "candidates": int(c[0]),
-              "useful_block_fraction": round(1 - c[6] / max(1, c[5]), 4),
-              "note": "counters build of the same sources (SKC_BITMAP_COUNTERS=1): a walked "
-                      "block is useful when at least one of its 32 q's was not already "
-                      "covered by STRICT"}
+              "useful_walk_fraction": round(1 - c[6] / max(1, c[5]), 4),
+              "note": "counters build of the same sources (SKC_BITMAP_COUNTERS=1): a walk "
+                      "step tests 32 q's (four 8-q sub-blocks whose minimum-cell boxes "
+                      "were not strict) and is useful when at least one of them was not "
+                      "already covered by STRICT"}
     cpath = os.path.join(REPO, "profiles", f"kernel_counters_{workload}.json")
     with open(cpath) as fh:
         t = json.load(fh)

@@ -19,8 +19,12 @@
 // of attributes where q may be <= p (LE subset of U). If U is in STRICT, the
 // down-closure of U is already strict and q adds nothing. The same test on
 // the byte-wise minimum cells of a block of 32 consecutive q's skips the
-// whole block. q's are ordered by the lattice level of their median mask so
-// the strongest points come first and STRICT fills early.
+// whole block (the box's U is the union of its q's U's), and on the minimum
+// cells of its four 8-q sub-blocks before a block is walked: on 1M x 10
+// anticorrelated, 89 % of the 32-q blocks that passed their box test held
+// no q that added anything, while 79 % of their 8-q sub-boxes were already
+// strict. q's are ordered by the lattice level of their median mask so the
+// strongest points come first and STRICT fills early.
 //
 // Mapping. One warp owns one p at a time (a persistent grid pulls p's from a
 // device counter) and its 32 lanes test 32 q's per step. For d <= 10 the
@@ -67,9 +71,10 @@ constexpr uint32_t kFull = 0xffffffffu;
 // (SKC_BITMAP_COUNTERS=1, skycube_gb300.build(counters=True)); the normal
 // build has none of this code. Per launch, summed over candidates:
 // [0] candidates, [1] partition ballots, [2] partitions visited, [3] box-test
-// steps, [4] block boxes tested, [5] blocks walked, [6] walked blocks whose
-// q's were all covered already, [7] STRICT updates, [8] tie pairs,
-// [9] q's tested that were not covered.
+// steps, [4] block boxes tested, [5] walk steps (32 q's), [6] walk steps whose
+// q's were all covered already, [7] STRICT updates, [8] tie pairs, [9] q's
+// tested that were not covered, [10] 8-q sub-boxes tested, [11] sub-blocks
+// opened.
 #if SKC_BITMAP_COUNTERS
 __device__ unsigned long long g_bitmap_counters[16];
 #define SKC_COUNT(i, v) (cnt_[i] += (v))
@@ -91,9 +96,12 @@ struct BitState {
   // list (E | L << 16) and applied directly when no more come; the global
   // map is used only when a candidate has more.
   static constexpr uint32_t LIST_WORDS = A_SMEM ? 0 : 32;
+  // The walk's lists, last: the open blocks of a box-test step (up to 32)
+  // and the open 8-q sub-blocks of a sub-box step (up to 32).
+  static constexpr uint32_t WALK_WORDS = 32 + 32;
   // shared memory per warp, in words
   static constexpr uint32_t SMEM_WORDS =
-      (REG ? 0 : W) + (A_SMEM ? AW : 0) + CHUNK_WORDS + LIST_WORDS;
+      (REG ? 0 : W) + (A_SMEM ? AW : 0) + CHUNK_WORDS + LIST_WORDS + WALK_WORDS;
 };
 
 // Splits the subsets of h over 32 lanes: `low` = the lowest five set bits of
@@ -345,7 +353,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
     const uint4* __restrict__ pcells, const float* __restrict__ px,
     uint64_t p_pad, const uint4* __restrict__ qcells,
     const float* __restrict__ qx, const uint4* __restrict__ bmin,
-    const uint32_t* __restrict__ boff, const uint32_t* __restrict__ unrank,
+    const uint4* __restrict__ smin, const uint32_t* __restrict__ boff, const uint32_t* __restrict__ unrank,
     uint32_t K, int B, int depth,
     const uint32_t* __restrict__ m_ptr, uint32_t* __restrict__ work, uint32_t chunk,
     uint32_t p_end_cap, uint32_t* __restrict__ out_dom,
@@ -362,6 +370,9 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   uint32_t* wsm = smem + (size_t)wib * BS::SMEM_WORDS;
+  uint32_t* wl = wsm + BS::SMEM_WORDS - BS::WALK_WORDS;  // open blocks of a box step
+  uint32_t* wo = wl + 32;                                // open sub-blocks of a sub-box step
+  const uint32_t lt_mask = (1u << lane) - 1u;
   uint32_t* sat_s = REG ? nullptr : wsm;
   uint32_t* A = BS::A_SMEM
                     ? wsm + (REG ? 0 : W)
@@ -375,7 +386,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
   constexpr uint32_t kCloseBlocks = W / 32;
 
 #if SKC_BITMAP_COUNTERS
-  unsigned long long cnt_[10] = {};
+  unsigned long long cnt_[12] = {};
 #endif
   for (;;) {
     // The warp takes `chunk` consecutive candidates per grab.
@@ -385,7 +396,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
     if (p0 >= pend) {
 #if SKC_BITMAP_COUNTERS
       if (lane == 0)
-        for (int i = 0; i < 10; ++i) atomicAdd(&g_bitmap_counters[i], cnt_[i]);
+        for (int i = 0; i < 12; ++i) atomicAdd(&g_bitmap_counters[i], cnt_[i]);
 #endif
       break;
     }
@@ -453,6 +464,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
         U |= pack_guards(ge_bytes(pH[w], word_of(q4, w))) << (4 * w);
       U &= NSUB - 1;
       const bool hit = in_strict(U);
+      SKC_COUNT(5, 1);
       if (__all_sync(kFull, hit)) {
         SKC_COUNT(6, 1);
         return;
@@ -624,20 +636,50 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
           Ub &= NSUB - 1;
         }
         const bool ub_strict = in_strict(Ub);  // every lane (shuffle)
-        uint32_t blocks = __ballot_sync(kFull, in_list && !ub_strict);
+        const uint32_t blocks = __ballot_sync(kFull, in_list && !ub_strict);
         SKC_COUNT(3, 1);
         SKC_COUNT(4, min(32u, total - t0));
-        SKC_COUNT(5, __popc(blocks));
-        if constexpr (CAP && !REG) since += 1 + __popc(blocks);
-        while (blocks) {
-          const int bs = __ffs(blocks) - 1;
-          blocks &= blocks - 1;
-          if constexpr (CAP && REG) {  // closed after every update
-            if (in_strict(__shfl_sync(kFull, Ub, bs))) continue;
+        if constexpr (CAP && !REG) since += 1;
+        if (!blocks) continue;
+        // The open blocks, compacted into the warp's list (previous readers
+        // are past the fence).
+        const uint32_t nb = __popc(blocks);
+        __syncwarp();
+        if ((blocks >> lane) & 1u) wl[__popc(blocks & lt_mask)] = kb;
+        __syncwarp();
+        for (uint32_t i0 = 0; i0 < nb; i0 += 8) {
+          // Sub-box tests: lane t takes 8-q sub-block t % 4 of open block
+          // i0 + t / 4, against STRICT as the walks so far left it.
+          const uint32_t slot = i0 + (lane >> 2);
+          const bool valid = slot < nb;
+          const uint32_t sid = wl[valid ? slot : nb - 1] * 4 + (lane & 3);
+          uint32_t Us = 0;
+          if (valid) {
+            const uint4 sm = smin[sid];
+#pragma unroll
+            for (int w = 0; w < NW; ++w)
+              Us |= pack_guards(ge_bytes(pH[w], word_of(sm, w))) << (4 * w);
+            Us &= NSUB - 1;
           }
-          // The q arrays are padded to whole blocks with entries that add
-          // nothing (k_pad_q), so every lane of a block can be tested.
-          test_q(__shfl_sync(kFull, kb, bs) * 32 + lane);
+          const bool us_strict = in_strict(Us);  // every lane (shuffle)
+          const uint32_t open = __ballot_sync(kFull, valid && !us_strict);
+          SKC_COUNT(10, min(8u, nb - i0) * 4);
+          SKC_COUNT(11, __popc(open));
+          if constexpr (CAP && !REG) since += 1;
+          if (!open) continue;
+          const uint32_t no = __popc(open);
+          __syncwarp();
+          if ((open >> lane) & 1u) wo[__popc(open & lt_mask)] = sid;
+          __syncwarp();
+          // Walks: four open sub-blocks per step, lane t on q t % 8 of
+          // sub-block j0 + t / 8; lanes past the last one repeat it (a q
+          // tested twice changes nothing). The q arrays are padded to whole
+          // blocks with entries that add nothing (k_pad_q).
+          for (uint32_t j0 = 0; j0 < no; j0 += 4) {
+            const uint32_t jj = min(j0 + (lane >> 3), no - 1);
+            test_q(wo[jj] * 8 + (lane & 7));
+            if constexpr (CAP && !REG) since += 1;
+          }
         }
       }
     }
@@ -754,7 +796,7 @@ static int launch_bitmaps_dc(cudaStream_t s, int num_sms, const BitmapArgs& a) {
   SKC_TRY((bitmap_grid_dc<D, CAP>(num_sms, &grid, &smem)));
   if (a.grid_blocks > 0 && a.grid_blocks < grid) grid = a.grid_blocks;
   k_bitmaps<D, CAP><<<grid, 256, smem, s>>>(a.pcells, a.px, a.p_pad, a.qcells, a.qx,
-                                             a.bmin, a.boff, a.unrank, a.K, a.B, a.depth,
+                                             a.bmin, a.smin, a.boff, a.unrank, a.K, a.B, a.depth,
                                              a.m_ptr, a.work, a.chunk ? a.chunk : 1u, a.p_end,
                                              a.out_dom, a.out_ext,
                                              a.tie_slab, a.cap, a.full_dom);

@@ -412,11 +412,12 @@ __global__ void k_gather_u4(const uint4* __restrict__ in,
     out[i] = in[perm[i]];
 }
 
-// Per block of 32 consecutive q's: byte-wise minimum of their cells. Padding
-// entries (index >= m) get cell 127 so they never lower the minimum.
+// Per block of 32 consecutive q's, and per 8-q quarter of it: byte-wise
+// minimum of their cells. Padding entries (index >= m) get cell 127 so they
+// never lower the minimum.
 __global__ void k_block_min(const uint4* __restrict__ cells,
                             const uint32_t* __restrict__ m_ptr,
-                            uint4* __restrict__ bmin) {
+                            uint4* __restrict__ bmin, uint4* __restrict__ smin) {
   const uint32_t m = *m_ptr;
   const uint32_t nblk = (m + 31) / 32;
   const int lane = threadIdx.x & 31;
@@ -424,11 +425,12 @@ __global__ void k_block_min(const uint4* __restrict__ cells,
        b += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t i = b * 32 + lane;
     uint4 c = i < m ? cells[i] : make_uint4(0x7f7f7f7fu, 0x7f7f7f7fu, 0x7f7f7f7fu, 0x7f7f7f7fu);
-    for (int o = 16; o; o >>= 1) {
+    for (int o = 1; o < 32; o <<= 1) {
       c.x = __vminu4(c.x, __shfl_xor_sync(0xffffffffu, c.x, o));
       c.y = __vminu4(c.y, __shfl_xor_sync(0xffffffffu, c.y, o));
       c.z = __vminu4(c.z, __shfl_xor_sync(0xffffffffu, c.z, o));
       c.w = __vminu4(c.w, __shfl_xor_sync(0xffffffffu, c.w, o));
+      if (o == 4 && (lane & 7) == 0) smin[(uint64_t)b * 4 + (lane >> 3)] = c;
     }
     if (lane == 0) bmin[b] = c;
   }
@@ -609,8 +611,8 @@ int launch_gather_u4(cudaStream_t s, const uint4* in, const uint32_t* perm,
 }
 
 int launch_block_min(cudaStream_t s, const uint4* cells, const uint32_t* m_ptr,
-                     uint64_t m_max, uint4* bmin) {
-  k_block_min<<<grid_for(m_max, 256, 152 * 8), 256, 0, s>>>(cells, m_ptr, bmin);
+                     uint64_t m_max, uint4* bmin, uint4* smin) {
+  k_block_min<<<grid_for(m_max, 256, 152 * 8), 256, 0, s>>>(cells, m_ptr, bmin, smin);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }
