@@ -293,7 +293,12 @@ static int run_full_space(Exec& E, skc_dataset* ds, const RunParams& P, Arena& A
   float* pivots;
   SKC_TRY(A.alloc(&pivots, (uint64_t)kMaxDims * kMaxPivots));
   SKC_TRY(A.alloc(&F.cells, n));
-  SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, nullptr, d_n, n, depth, pivots, F.cells));
+  // The cells kernel also sums the points' cell sums and their squares: the
+  // spread that picks the skyline kernel's order (partition.cu, gray_order).
+  unsigned long long* spread;
+  SKC_TRY(A.alloc(&spread, 3));
+  SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, nullptr, d_n, n, depth, pivots, F.cells,
+                              spread));
   T.mark("full: pivots+cells");
 
   // Pruner prefilter: the skyline kernel then runs over the survivors only
@@ -343,13 +348,17 @@ static int run_full_space(Exec& E, skc_dataset* ds, const RunParams& P, Arena& A
   SKC_TRY(A.alloc(&ps.cursor, kMaxSortBuckets + 1));
   SKC_TRY(A.alloc(&ps.fine, kMaxSortBuckets + 1));
   SKC_TRY(A.alloc(&ps.items, K + 1));
+  ps.spread = spread;
   uint8_t* status;
   SKC_TRY(A.alloc(&status, round_up(n, 4)));
   PartitionSkylineArgs pa{list, F.cells, ds->x, ds->n_pad, m_list, n, full, status};
   // Slices pay on candidate-dense lists (the survivors); on lists full of
   // dominated points the slices after the strongest partitions would run to
   // their end for points the first slice already settles.
-  if (list) pa.split_target = (uint32_t)ctx->num_sms * kSplitCtasPerSm;
+  if (list) {
+    pa.split_target = (uint32_t)ctx->num_sms * kSplitCtasPerSm;
+    pa.spread_ready = true;  // the spread of all n points picks the order
+  }
   SKC_TRY(launch_partition_skyline(s, d, depth, LT, pa, ps));
   T.mark("full: skyline kernel");
 
@@ -1447,6 +1456,7 @@ static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, const RunPara
     SKC_TRY(A.alloc(&ps.cursor, kMaxSortBuckets + 1));
     SKC_TRY(A.alloc(&ps.fine, kMaxSortBuckets + 1));
     SKC_TRY(A.alloc(&ps.items, K + 1));
+    SKC_TRY(A.alloc(&ps.spread, 3));
     if (m >= kConfirmedMinPoints) {
       SKC_TRY(A.alloc(&ps.conf_cells, m));
       SKC_TRY(A.alloc(&ps.conf_x, (uint64_t)d * round_up(m, 128)));
@@ -1490,7 +1500,11 @@ static int run_single_cuboid(Exec& E, skc_dataset* ds, uint32_t S, const RunPara
       m_ptr = d_ns;
     }
     PartitionSkylineArgs pa{list, F.cells, ds->x, ds->n_pad, m_ptr, m, S, status};
-    if (filter) pa.split_target = (uint32_t)E.ctx->num_sms * kSplitCtasPerSm;
+    if (filter) {
+      pa.split_target = (uint32_t)E.ctx->num_sms * kSplitCtasPerSm;
+      pa.spread_ids = F.cand;  // the spread of the candidates on S picks the order
+      pa.spread_m = F.counts + 2;
+    }
     SKC_TRY(launch_partition_skyline(s, d, depth, LT, pa, ps));
     SKC_TRY(launch_status_compact(s, status, list, m_ptr, m, 0, blk0, blk1, sky, ext, cnt, cnt + 1));
     uint32_t h[2] = {0, 0};

@@ -30,7 +30,8 @@ int launch_counting_sort(cudaStream_t s, const uint32_t* keys,
                          const BucketScratch& b, uint32_t* sorted, uint32_t* hi);
 int launch_pivots_cells(cudaStream_t s, const float* x, uint64_t n_pad, int d,
                         const uint32_t* ids, const uint32_t* m_ptr,
-                        uint64_t m_max, int depth, float* pivots, uint4* cells);
+                        uint64_t m_max, int depth, float* pivots, uint4* cells,
+                        unsigned long long* spread = nullptr);
 int launch_status_compact(cudaStream_t s, const uint8_t* st, const uint32_t* ids,
                           const uint32_t* m_ptr, uint64_t m_max, int merge01,
                           uint32_t* blk0, uint32_t* blk1, uint32_t* out0,
@@ -111,6 +112,11 @@ struct PartScratch {
   uint32_t* fine;    // [kMaxSortBuckets + 1] counting-sort offsets
   uint32_t* cursor;  // [kMaxSortBuckets + 1]
   uint32_t* items;   // [2^B + 1]
+  // Spread of the cell sums of the list before the prefilter (sum, sum of
+  // squares, count), for sliced lists; nullptr: strength order, no tile box.
+  // Zeroed by k_pivots and filled by k_cells when launch_pivots_cells is
+  // given it.
+  unsigned long long* spread = nullptr;  // [3]
 };
 struct PartitionSkylineArgs {
   const uint32_t* ids;  // list position -> point id (nullptr: identity)
@@ -122,6 +128,11 @@ struct PartitionSkylineArgs {
   uint32_t S;
   uint8_t* status;      // list position -> status; m_max rounded up to 4 bytes
   uint32_t split_target = 0;  // CTAs the skyline kernel's work is cut into (0: no slicing)
+  // Sliced lists: the list whose cell-sum spread picks the order inside the
+  // partitions (point ids, nullptr: 0 .. count - 1; count on the device).
+  const uint32_t* spread_ids = nullptr;
+  const uint32_t* spread_m = nullptr;
+  bool spread_ready = false;  // PartScratch::spread already holds the spread
 };
 // Skyline kernel: CTAs per SM the work is balanced over (split_target).
 constexpr uint32_t kSplitCtasPerSm = 32;

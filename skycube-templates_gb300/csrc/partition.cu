@@ -23,6 +23,71 @@
 
 namespace skc {
 
+// Order inside the partitions of a sliced skyline list. The strength order
+// (cell sum) lets a dominated point meet a dominator early; the Gray order
+// keeps q tiles' minimum-cell boxes tight, so whole tiles are skipped. Which
+// wins follows the spread of the points' cell sums: where they are
+// concentrated (anticorrelated data, points near a hyperplane) the strength
+// order carries little and the Gray order wins; where they spread as much
+// as independent attributes would, or more, the strength order wins.
+// Measured (skyline kernel, strength -> Gray + tile boxes): anticorrelated
+// 1M x 10 7.03 -> 5.99 ms, 400k x 12 3.77 -> 3.48 ms, 200k x 8 0.50 -> 0.44
+// ms (spread 0.51-0.62 of the independent value); uniform 1M x 10 1.74 ->
+// 1.80 ms, 500k x 16 6.38 -> 6.57 ms (1.01); correlated 1M x 10 2.47 ->
+// 3.61 ms, quantised 566k x 15 1.31 -> 1.93 ms (3.1-3.8). Only the
+// partition part of the key matters for correctness. With the choice made
+// on the device (both skyline instantiations launched, one returning at
+// once): anticorrelated 1M x 10 6.90 -> 5.93 ms, 400k x 12 3.74 -> 3.47 ms,
+// 500k x 16 8.48 -> 8.14 ms; the others within 1 %.
+constexpr double kGraySpread = 0.8;  // limit, as a fraction of the independent spread
+// Below this many points the choice is not made (strength order): the
+// second skyline launch it needs costs about 13 us, more than the Gray
+// order gains on such lists.
+constexpr uint64_t kSpreadMinPoints = 1u << 17;
+
+// spread[0] += sum over list entries of the cell sum over S, spread[1] += its
+// square, spread[2] = the count. Cell sums are at most 16 * 127, so both
+// sums fit 64 bits for any list of 32-bit length.
+__global__ void k_cell_spread(const uint4* __restrict__ cells, const uint32_t* __restrict__ ids,
+                              const uint32_t* __restrict__ m_ptr, uint32_t S, int d,
+                              unsigned long long* __restrict__ spread) {
+  const uint32_t m = *m_ptr;
+  unsigned long long s1 = 0, s2 = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += gridDim.x * blockDim.x) {
+    const uint4 c = cells[ids ? ids[i] : i];
+    uint32_t sum = 0;
+    for (int k = 0; k < d; ++k)
+      if (S & (1u << k)) sum += (word_of(c, k >> 2) >> (8 * (k & 3))) & 0x7fu;
+    s1 += sum;
+    s2 += (unsigned long long)sum * sum;
+  }
+  for (int o = 16; o; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  if ((threadIdx.x & 31) == 0 && s1) {
+    atomicAdd(&spread[0], s1);
+    atomicAdd(&spread[1], s2);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) spread[2] = m;
+}
+
+// Gray order when the variance of the cell sums is below `limit`
+// (kGraySpread^2 times the variance of a sum of |S| independent uniform
+// cells). Every thread of the sort and skyline kernels evaluates it, so it
+// is single precision (FP64 is a slow pipe here: in double it cost 80 us on
+// 100k points); the variance is in the thousands and its rounding error
+// below 0.1.
+__device__ __forceinline__ bool gray_order(const unsigned long long* spread, float limit) {
+  const unsigned long long n = spread[2];
+  if (n < 2) return false;
+  const float inv = 1.0f / (float)n;
+  const float mean = (float)spread[0] * inv;
+  const float var = (float)spread[1] * inv - mean * mean;
+  return var < limit;
+}
+
 // key[i] = rank of the median mask of list entry i over the first B
 // attributes of S, times 2^sub_bits, plus (when sub_bits > 0) the sum of its
 // grid cells over S scaled to sub_bits bits. Sorting by the key groups
@@ -35,14 +100,18 @@ namespace skc {
 // one attribute and any run of them varies in few. Consecutive points then
 // share their quartile on most attributes, which keeps the minimum-cell
 // boxes of 32-point blocks tight. Only the partition part matters for
-// correctness.
+// correctness. Sub_mode 2 takes the Gray order when the list's cell sums
+// are concentrated (gray_order below) and the strength order otherwise.
 __global__ void k_mask_keys(const uint4* __restrict__ cells,
                             const uint32_t* __restrict__ ids,
                             const uint32_t* __restrict__ m_ptr, uint32_t S,
                             int d, int B, int depth, int sub_bits, int sub_mode,
                             const uint32_t* __restrict__ rank,
-                            uint32_t* __restrict__ keys) {
+                            uint32_t* __restrict__ keys,
+                            const unsigned long long* __restrict__ spread,
+                            float spread_limit) {
   const uint32_t m = *m_ptr;
+  if (sub_mode == 2) sub_mode = gray_order(spread, spread_limit) ? 1 : 0;
   const int sh = depth - 1;
   const uint32_t cmax = (1u << depth) - 1;
   const uint32_t span = cmax * (uint32_t)__popc(S);
@@ -141,6 +210,10 @@ struct PartKernelArgs {
   const uint32_t* cta_off;  // first CTA of partition b [K + 1]
   uint32_t lvl_mul;         // strength level = cell sum * lvl_mul / lvl_span
   uint32_t lvl_span;        //   (the sort's sub-key, k_mask_keys); 0: no cut
+  // Sliced lists: the cell-sum spread and its limit (gray_order); when the
+  // partitions are in Gray order, q tiles are box-tested (nullptr: never).
+  const unsigned long long* spread;
+  float spread_limit;
 };
 
 // Cell sum of compact cells over NA attributes (the sort's strength level
@@ -247,9 +320,14 @@ constexpr uint32_t kFullMask = 0xffffffffu;
 // no spill; it had taken 48 and 5 CTAs): 1M x 10 anticorrelated full
 // skycube 28.4 -> 27.7 ms. Above 10 attributes the bound would spill, and
 // the unsliced level-cutoff variant (LV) keeps the free register budget.
-template <int NA, bool LV>
+// BOX (sliced lists only): q tiles are box-tested. Both instantiations are
+// launched for a sliced list whose order follows the spread, and the one
+// that does not match the device's choice (gray_order) returns at once: a
+// runtime switch kept both paths' registers live and spilled at 40.
+template <int NA, bool LV, bool BOX>
 __global__ void __launch_bounds__(256, (!LV && NA <= 10) ? 6 : 1) k_skyline_part(PartKernelArgs a) {
   constexpr int NW = (NA + 3) / 4;
+  if (a.spread != nullptr && gray_order(a.spread, a.spread_limit) != BOX) return;
   constexpr int TQ = 256;
   __shared__ uint4 q_cells[TQ];
   __shared__ float q_x[NA][TQ];
@@ -451,6 +529,13 @@ __global__ void __launch_bounds__(256, (!LV && NA <= 10) ? 6 : 1) k_skyline_part
   // arrays and stops on its own: no CTA barrier inside the loop, so a warp
   // whose points are all settled does not wait for the slowest warp.
   const int lane = threadIdx.x & 31;
+  // In Gray order a tile's q's share their quartile on most attributes, so
+  // its byte-wise minimum cells often lie above a point's cell somewhere;
+  // a point below the minimum on some attribute is dominated by no q of the
+  // tile, and a tile no point of the warp can be dominated by is skipped.
+  // In strength order the boxes are loose and the test only costs
+  // (1M x 10 anticorrelated: 6.9 -> 8.3 ms).
+  constexpr bool box = BOX;
   const uint32_t wbase = threadIdx.x & ~31u;  // this warp's slice
   bool wdone = false;  // every point of the warp is settled
   for (uint32_t si = s0; si < s1 && !wdone && acc < s_hi; ++si) {
@@ -496,10 +581,10 @@ __global__ void __launch_bounds__(256, (!LV && NA <= 10) ? 6 : 1) k_skyline_part
       }
       first = false;
       const uint32_t j = base + lane;
+      uint4 qcl = make_uint4(0x7f7f7f7fu, 0x7f7f7f7fu, 0x7f7f7f7fu, 0x7f7f7f7fu);
       if (j < qend) {
         // Confirmed lists are written during this launch by other SMs: read
         // them through L2 (ld.cg), never from a possibly stale L1 line.
-        uint4 qcl;
         if (conf) {
           qcl = __ldcg(qc + j);
 #pragma unroll
@@ -512,8 +597,20 @@ __global__ void __launch_bounds__(256, (!LV && NA <= 10) ? 6 : 1) k_skyline_part
         q_cells[threadIdx.x] = qcl;
         if constexpr (LV) q_sum[threadIdx.x] = (uint16_t)cell_sum_na<NA>(qcl);
       }
+      bool box_out = false;  // no q of the tile dominates this point
+      if constexpr (box) {
+        uint32_t worse = 0;  // guard bits where the minimum cell is above p's
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {  // one word at a time: few live registers
+          uint32_t mn = word_of(qcl, w);
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) mn = __vminu4(mn, __shfl_xor_sync(kFullMask, mn, o));
+          worse |= ~(pH[w] - mn) & hS[w];
+        }
+        box_out = worse != 0;
+      }
       __syncwarp();
-      if (!done && !(LV && beyond)) {
+      if (!done && !(LV && beyond) && !box_out) {
         uint32_t lim = min(32u, qend - base);
         if (LV && !conf && sum_cut != 0xffffffffu) {
           // First q of the tile above p's level (levels ascend in a sorted
@@ -593,7 +690,8 @@ int launch_mask_keys(cudaStream_t s, const uint4* cells, const uint32_t* ids,
                      int B, int depth, int sub_bits, int sub_mode, const uint32_t* rank,
                      uint32_t* keys) {
   k_mask_keys<<<blocks_for(m_max, 256, 152 * 8), 256, 0, s>>>(cells, ids, m_ptr, S, d, B, depth,
-                                                               sub_bits, sub_mode, rank, keys);
+                                                               sub_bits, sub_mode, rank, keys,
+                                                               nullptr, 0.0f);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }
@@ -626,8 +724,22 @@ int launch_partition_skyline(cudaStream_t s, int d, int depth,
   bs.keys = ps.keys;
   bs.counts = ps.fine;
   bs.cursor = ps.cursor;
+  // Sliced lists: the order inside the partitions by the spread of the
+  // cell sums over the list before the prefilter (gray_order).
+  const bool by_spread = a.split_target && depth >= 2 && ps.spread &&
+                         (a.spread_m || a.spread_ready) && a.m_max >= kSpreadMinPoints;
+  const uint32_t c1 = 1u << depth;  // cells per attribute
+  const float spread_limit =
+      (float)(kGraySpread * kGraySpread * (double)na * ((double)c1 * c1 - 1.0) / 12.0);
+  if (by_spread && !a.spread_ready) {
+    SKC_CUDA(cudaMemsetAsync(ps.spread, 0, 3 * sizeof(unsigned long long), s));
+    k_cell_spread<<<blocks_for(a.m_max, 256, 152 * 4), 256, 0, s>>>(
+        a.cells, a.spread_ids, a.spread_m, a.S, d, ps.spread);
+    SKC_LAUNCH_CHECK();
+  }
   k_mask_keys<<<blocks_for(a.m_max, 256, 152 * 8), 256, 0, s>>>(
-      a.cells, a.ids, a.m_ptr, a.S, d, T.B, depth, sub_bits, 0, T.rank, ps.keys);
+      a.cells, a.ids, a.m_ptr, a.S, d, T.B, depth, sub_bits, by_spread ? 2 : 0, T.rank, ps.keys,
+      ps.spread, spread_limit);
   SKC_LAUNCH_CHECK();
   SKC_TRY(launch_counting_sort(s, ps.keys, a.m_ptr, a.m_max, KB, bs, ps.sorted, nullptr));
   k_partition_offsets<<<blocks_for(K + 1, 256, 64), 256, 0, s>>>(ps.fine, K, sub_bits, ps.counts);
@@ -653,7 +765,8 @@ int launch_partition_skyline(cudaStream_t s, int d, int depth,
                    // prefilter); on candidate-dense, sliced lists they only
                    // cost (581k x 10 ties survivors: 3.05 -> 3.43 ms).
                    a.split_target ? 0u : (1u << sub_bits) - 1u,
-                   ((1u << depth) - 1u) * (uint32_t)na};
+                   ((1u << depth) - 1u) * (uint32_t)na,
+                   by_spread ? ps.spread : nullptr, spread_limit};
   // Split CTAs OR their statuses in: start from zero (the buffer is padded
   // to a multiple of 4 bytes).
   SKC_CUDA(cudaMemsetAsync(a.status, 0, (a.m_max + 3) & ~3ull, s));
@@ -664,12 +777,14 @@ int launch_partition_skyline(cudaStream_t s, int d, int depth,
   // Upper bound of the CTAs k_split_plan hands out: sum over items of
   // ceil(work / W) <= target + items.
   const unsigned grid = (unsigned)((a.m_max + 255) / 256 + K + a.split_target);
-#define SKC_PART_CASE(N)                                  \
-  case N:                                                 \
-    if (k.lvl_mul)                                        \
-      k_skyline_part<N, true><<<grid, 256, 0, s>>>(k);    \
-    else                                                  \
-      k_skyline_part<N, false><<<grid, 256, 0, s>>>(k);   \
+#define SKC_PART_CASE(N)                                           \
+  case N:                                                          \
+    if (k.lvl_mul) {                                               \
+      k_skyline_part<N, true, false><<<grid, 256, 0, s>>>(k);      \
+    } else {                                                       \
+      if (by_spread) k_skyline_part<N, false, true><<<grid, 256, 0, s>>>(k); \
+      k_skyline_part<N, false, false><<<grid, 256, 0, s>>>(k);     \
+    }                                                              \
     break;
   switch (na) {
     SKC_PART_CASE(1) SKC_PART_CASE(2) SKC_PART_CASE(3) SKC_PART_CASE(4)

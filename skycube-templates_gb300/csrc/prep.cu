@@ -184,9 +184,11 @@ constexpr int kPivotSample = 4096;
 
 __global__ void __launch_bounds__(1024) k_pivots(
     const float* __restrict__ x, uint64_t n_pad, const uint32_t* __restrict__ ids,
-    const uint32_t* __restrict__ m_ptr, int depth, float* __restrict__ pivots) {
+    const uint32_t* __restrict__ m_ptr, int depth, float* __restrict__ pivots,
+    unsigned long long* __restrict__ spread) {
   __shared__ float s[kPivotSample];
   const int k = blockIdx.x;
+  if (spread && k == 0 && threadIdx.x < 3) spread[threadIdx.x] = 0;  // k_cells adds to it
   const uint32_t m = *m_ptr;
   const uint32_t cnt = m < kPivotSample ? m : kPivotSample;
   for (int t = threadIdx.x; t < kPivotSample; t += blockDim.x) {
@@ -224,20 +226,25 @@ __global__ void __launch_bounds__(1024) k_pivots(
 }
 
 // cells[i] = grid cells of point ids[i] (see common.cuh).
+// With `spread`, also the sum and the sum of squares of the points' cell
+// sums and their count (k_cell_spread's layout, every attribute).
 __global__ void k_cells(const float* __restrict__ x, uint64_t n_pad,
                         const uint32_t* __restrict__ ids,
                         const uint32_t* __restrict__ m_ptr, int d, int depth,
                         const float* __restrict__ pivots,
-                        uint4* __restrict__ cells) {
+                        uint4* __restrict__ cells,
+                        unsigned long long* __restrict__ spread) {
   __shared__ float piv[kMaxDims * kMaxPivots];
   for (int t = threadIdx.x; t < d * kMaxPivots; t += blockDim.x) piv[t] = pivots[t];
   __syncthreads();
   const uint32_t m = *m_ptr;
   const int P = (1 << depth) - 1;
+  unsigned long long s1 = 0, s2 = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m;
        i += gridDim.x * blockDim.x) {
     const uint32_t id = ids ? ids[i] : i;
     uint32_t w[4] = {0, 0, 0, 0};
+    uint32_t sum = 0;
     for (int k = 0; k < d; ++k) {
       const float v = x[(uint64_t)k * n_pad + id];
       const float* pk = piv + k * kMaxPivots;
@@ -247,8 +254,22 @@ __global__ void k_cells(const float* __restrict__ x, uint64_t n_pad,
         if (pk[mid] < v) lo = mid + 1; else hi = mid;
       }
       w[k >> 2] |= (uint32_t)lo << (8 * (k & 3));
+      sum += (uint32_t)lo;
     }
     cells[i] = make_uint4(w[0], w[1], w[2], w[3]);
+    s1 += sum;
+    s2 += (unsigned long long)sum * sum;
+  }
+  if (spread) {
+    for (int o = 16; o; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if ((threadIdx.x & 31) == 0 && s1) {
+      atomicAdd(&spread[0], s1);
+      atomicAdd(&spread[1], s2);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) spread[2] = m;
   }
 }
 
@@ -547,10 +568,12 @@ int launch_counting_sort(cudaStream_t s, const uint32_t* keys,
 
 int launch_pivots_cells(cudaStream_t s, const float* x, uint64_t n_pad, int d,
                         const uint32_t* ids, const uint32_t* m_ptr,
-                        uint64_t m_max, int depth, float* pivots, uint4* cells) {
-  k_pivots<<<d, 1024, 0, s>>>(x, n_pad, ids, m_ptr, depth, pivots);
+                        uint64_t m_max, int depth, float* pivots, uint4* cells,
+                        unsigned long long* spread) {
+  k_pivots<<<d, 1024, 0, s>>>(x, n_pad, ids, m_ptr, depth, pivots, spread);
   SKC_LAUNCH_CHECK();
-  k_cells<<<grid_for(m_max, 256, 152 * 8), 256, 0, s>>>(x, n_pad, ids, m_ptr, d, depth, pivots, cells);
+  k_cells<<<grid_for(m_max, 256, 152 * 8), 256, 0, s>>>(x, n_pad, ids, m_ptr, d, depth, pivots,
+                                                         cells, spread);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }
