@@ -809,7 +809,7 @@ def record_useful(workload):
     ctx = sk.Context(0)
     ds = sk.Dataset(ctx, datagen.generate(kind, n, d, seed))
     sk.skycube(ctx, ds, "mdmc", "batched", max_d=max_d).close()
-    c = (ctypes.c_ulonglong * 16)()
+    c = (ctypes.c_ulonglong * 32)()
     f(c, 1)
     sk.skycube(ctx, ds, "mdmc", "batched", max_d=max_d).close()
     f(c, 0)
@@ -817,7 +817,8 @@ def record_useful(workload):
     names = ["candidates", "partition_ballots", "partitions_visited", "box_test_steps",
              "block_boxes_tested", "walk_steps", "walk_steps_all_covered",
              "strict_updates", "tie_pairs", "uncovered_q_tested", "sub_boxes_tested",
-             "sub_blocks_opened"]
+             "sub_blocks_opened", "cycles_partition_ballots", "cycles_box_tests",
+             "cycles_quarter_box_tests", "cycles_walks", "cycles_candidate", "cycles_output"]
     useful = {"per_candidate": {nm: round(c[i] / m, 3) for i, nm in enumerate(names) if i},
               "candidates": int(c[0]),
               "useful_walk_fraction": round(1 - c[6] / max(1, c[5]), 4),

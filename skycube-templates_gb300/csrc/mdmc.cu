@@ -74,12 +74,36 @@ constexpr uint32_t kFull = 0xffffffffu;
 // steps, [4] block boxes tested, [5] walk steps (32 q's), [6] walk steps whose
 // q's were all covered already, [7] STRICT updates, [8] tie pairs, [9] q's
 // tested that were not covered, [10] 8-q sub-boxes tested, [11] sub-blocks
-// opened.
+// opened; SM cycles (clock64, per warp, summed) spent in [12] partition
+// ballots, [13] box tests, [14] quarter-box tests, [15] walks, [16] the
+// whole candidate and [17] its output.
+constexpr int kBitmapCounters = 18;
 #if SKC_BITMAP_COUNTERS
-__device__ unsigned long long g_bitmap_counters[16];
+__device__ unsigned long long g_bitmap_counters[kBitmapCounters];
 #define SKC_COUNT(i, v) (cnt_[i] += (v))
+#define SKC_T0(v) const long long v = clock64()
+#define SKC_TADD(i, v) (cnt_[i] += (unsigned long long)(clock64() - (v)))
+// Adds the cycles from its construction to the end of its scope.
+struct CycleScope {
+  unsigned long long* acc;
+  long long t0 = 0;
+  __device__ explicit CycleScope(unsigned long long* a) : acc(a) {
+#ifdef __CUDA_ARCH__
+    t0 = clock64();
+#endif
+  }
+  __device__ ~CycleScope() {
+#ifdef __CUDA_ARCH__
+    *acc += (unsigned long long)(clock64() - t0);
+#endif
+  }
+};
+#define SKC_SCOPE(name, i) CycleScope name(&cnt_[i])
 #else
 #define SKC_COUNT(i, v) ((void)0)
+#define SKC_T0(v) ((void)0)
+#define SKC_TADD(i, v) ((void)0)
+#define SKC_SCOPE(name, i) ((void)0)
 #endif
 
 template <int D>
@@ -386,7 +410,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
   constexpr uint32_t kCloseBlocks = W / 32;
 
 #if SKC_BITMAP_COUNTERS
-  unsigned long long cnt_[12] = {};
+  unsigned long long cnt_[kBitmapCounters] = {};
 #endif
   for (;;) {
     // The warp takes `chunk` consecutive candidates per grab.
@@ -396,7 +420,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
     if (p0 >= pend) {
 #if SKC_BITMAP_COUNTERS
       if (lane == 0)
-        for (int i = 0; i < 12; ++i) atomicAdd(&g_bitmap_counters[i], cnt_[i]);
+        for (int i = 0; i < kBitmapCounters; ++i) atomicAdd(&g_bitmap_counters[i], cnt_[i]);
 #endif
       break;
     }
@@ -418,6 +442,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
     // STRICT starts with the empty subspace so that q's worse on every
     // attribute (U == 0) test as "nothing new".
     SKC_COUNT(0, 1);
+    SKC_SCOPE(cs_cand, 16);
     uint32_t sat = 0;
     if (REG) {
       sat = (wi == 0) ? 1u : 0u;
@@ -574,6 +599,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
     // (all but those where the partition is above the median and p is not)
     // already form a strictly dominated subspace.
     for (uint32_t b0 = 0; b0 < K; b0 += 32) {
+      SKC_T0(t_part);
       maybe_close();
       if constexpr (CAP) {  // every subspace within the cap is strict
         if (in_strict(NSUB - 1)) break;
@@ -591,7 +617,10 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
       const uint32_t parts = __ballot_sync(kFull, sel);
       SKC_COUNT(1, 1);
       SKC_COUNT(2, __popc(parts));
-      if (!parts) continue;
+      if (!parts) {
+        SKC_TADD(12, t_part);
+        continue;
+      }
       // The blocks of all selected partitions form one list, so their box
       // tests fill the 32 lanes: lane t's partition owns blocks [bf, be).
       // A block shared with the previous selected partition (or visited
@@ -613,7 +642,9 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
       next_blk = max(next_blk, __shfl_sync(kFull, be, 31 - __clz(parts)));
       // list entry g of lane t's partition is block g + base (mod 2^32)
       const uint32_t base = bf - (incl - cnt);
+      SKC_TADD(12, t_part);
       for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+        SKC_T0(t_box);
         maybe_close();
         const uint32_t g = t0 + lane;
         // owner of list entry g: the first lane whose inclusive sum is > g
@@ -640,14 +671,19 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
         SKC_COUNT(3, 1);
         SKC_COUNT(4, min(32u, total - t0));
         if constexpr (CAP && !REG) since += 1;
-        if (!blocks) continue;
+        if (!blocks) {
+          SKC_TADD(13, t_box);
+          continue;
+        }
         // The open blocks, compacted into the warp's list (previous readers
         // are past the fence).
         const uint32_t nb = __popc(blocks);
         __syncwarp();
         if ((blocks >> lane) & 1u) wl[__popc(blocks & lt_mask)] = kb;
         __syncwarp();
+        SKC_TADD(13, t_box);
         for (uint32_t i0 = 0; i0 < nb; i0 += 8) {
+          SKC_T0(t_sub);
           // Sub-box tests: lane t takes 8-q sub-block t % 4 of open block
           // i0 + t / 4, against STRICT as the walks so far left it.
           const uint32_t slot = i0 + (lane >> 2);
@@ -666,18 +702,24 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
           SKC_COUNT(10, min(8u, nb - i0) * 4);
           SKC_COUNT(11, __popc(open));
           if constexpr (CAP && !REG) since += 1;
-          if (!open) continue;
+          if (!open) {
+            SKC_TADD(14, t_sub);
+            continue;
+          }
           const uint32_t no = __popc(open);
           __syncwarp();
           if ((open >> lane) & 1u) wo[__popc(open & lt_mask)] = sid;
           __syncwarp();
+          SKC_TADD(14, t_sub);
           // Walks: four open sub-blocks per step, lane t on q t % 8 of
           // sub-block j0 + t / 8; lanes past the last one repeat it (a q
           // tested twice changes nothing). The q arrays are padded to whole
           // blocks with entries that add nothing (k_pad_q).
           for (uint32_t j0 = 0; j0 < no; j0 += 4) {
             const uint32_t jj = min(j0 + (lane >> 3), no - 1);
+            SKC_T0(t_walk);
             test_q(wo[jj] * 8 + (lane & 7));
+            SKC_TADD(15, t_walk);
             if constexpr (CAP && !REG) since += 1;
           }
         }
@@ -686,6 +728,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
 
     // Output: dominated = STRICT | TIE, extended = TIE \ STRICT, with TIE
     // from the closed tie map. Bit 0 (the empty subspace) is cleared.
+    SKC_SCOPE(cs_out, 17);
     if constexpr (!BS::A_SMEM) {
       if (tmode == 2) {
         __syncwarp();
@@ -835,13 +878,13 @@ static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
   }
 
 #if SKC_BITMAP_COUNTERS
-// Counters build only: copies the summed counters out and, when reset is
-// nonzero, zeroes them.
+// Counters build only: copies the kBitmapCounters (18) summed counters out
+// (`out` holds at least that many) and, when reset is nonzero, zeroes them.
 extern "C" int skc_debug_bitmap_counters(unsigned long long* out, int reset) {
   if (cudaMemcpyFromSymbol(out, g_bitmap_counters, sizeof(g_bitmap_counters)) != cudaSuccess)
     return SKC_ERR_CUDA;
   if (reset) {
-    unsigned long long z[16] = {};
+    unsigned long long z[kBitmapCounters] = {};
     if (cudaMemcpyToSymbol(g_bitmap_counters, z, sizeof(z)) != cudaSuccess) return SKC_ERR_CUDA;
   }
   return SKC_OK;
