@@ -507,7 +507,24 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
         const uint32_t Z = U & G;   // equal cells: compare the floats
         le = Y;
         lt = Y;
-        if (Z) {
+        // The warp runs the union of its lanes' work: the unrolled form
+        // costs all D predicated steps whenever any lane has a cell tie, the
+        // loop only as many as the lane with the most ties. Measured on one
+        // box (bitmap kernel, identical outputs): 1M x 10 13.53 -> 11.65 ms,
+        // 400k x 12 33.7 -> 31.9 ms, 400k x 12 -m 6 23.06 -> 21.73 ms, 300k x
+        // 14 51.2 -> 49.0 ms; capped above 12 attributes the loop lost
+        // (500k x 16 -m 6 242.7 -> 249.0 ms, -m 8 434 -> 450 ms), and those
+        // keep the unrolled form.
+        if constexpr (!CAP || D <= 12) {
+          for (uint32_t z = Z; z; z &= z - 1) {
+            const int k = __ffs(z) - 1;
+            const float a = qx[(uint64_t)k * p_pad + qi];
+            const float b = pxp[(uint64_t)k * p_pad];
+            const uint32_t bit = 1u << k;
+            if (a <= b) le |= bit;
+            if (a < b) lt |= bit;
+          }
+        } else if (Z) {
 #pragma unroll
           for (int k = 0; k < D; ++k) {
             if (Z & (1u << k)) {
