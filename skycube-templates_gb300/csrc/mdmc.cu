@@ -120,9 +120,11 @@ struct BitState {
   // list (E | L << 16) and applied directly when no more come; the global
   // map is used only when a candidate has more.
   static constexpr uint32_t LIST_WORDS = A_SMEM ? 0 : 32;
-  // The walk's lists, last: the open blocks of a box-test step (up to 32)
-  // and the open 8-q sub-blocks of a sub-box step (up to 32).
-  static constexpr uint32_t WALK_WORDS = 32 + 32;
+  // The walk's queues, last: open blocks (up to 7 waiting + 32 from a
+  // box-test step) and open 8-q sub-blocks (up to 3 waiting + 32 from a
+  // sub-box step).
+  static constexpr uint32_t BQ_WORDS = 40, WQ_WORDS = 36;
+  static constexpr uint32_t WALK_WORDS = BQ_WORDS + WQ_WORDS;
   // shared memory per warp, in words
   static constexpr uint32_t SMEM_WORDS =
       (REG ? 0 : W) + (A_SMEM ? AW : 0) + CHUNK_WORDS + LIST_WORDS + WALK_WORDS;
@@ -394,8 +396,8 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   uint32_t* wsm = smem + (size_t)wib * BS::SMEM_WORDS;
-  uint32_t* wl = wsm + BS::SMEM_WORDS - BS::WALK_WORDS;  // open blocks of a box step
-  uint32_t* wo = wl + 32;                                // open sub-blocks of a sub-box step
+  uint32_t* bq = wsm + BS::SMEM_WORDS - BS::WALK_WORDS;  // open blocks, waiting
+  uint32_t* wq = bq + BS::BQ_WORDS;                      // open sub-blocks, waiting
   const uint32_t lt_mask = (1u << lane) - 1u;
   uint32_t* sat_s = REG ? nullptr : wsm;
   uint32_t* A = BS::A_SMEM
@@ -610,6 +612,55 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
       }
     };
 
+    // Open blocks and open 8-q sub-blocks wait in per-warp stacks until a
+    // full step's worth is there (8 blocks' quarters per sub-box step, 4
+    // sub-blocks per walk step), so steps stay full across box-test steps;
+    // the order they are taken in does not matter for the result.
+    uint32_t bq_n = 0, wq_n = 0;
+    // Walk step over the top c (<= 4) waiting sub-blocks: lane t on q t % 8
+    // of sub-block t / 8; lanes past the last one repeat it (a q tested
+    // twice changes nothing). The q arrays are padded to whole blocks with
+    // entries that add nothing (k_pad_q).
+    auto walk_step = [&](uint32_t c) {
+      SKC_T0(t_walk);
+      const uint32_t jj = min((uint32_t)(lane >> 3), c - 1);
+      const uint32_t qi = wq[wq_n - c + jj] * 8 + (lane & 7);
+      wq_n -= c;
+      __syncwarp();  // read before a later push overwrites the entry
+      test_q(qi);
+      SKC_TADD(15, t_walk);
+      if constexpr (CAP && !REG) since += 1;
+    };
+    // Sub-box step over the top c (<= 8) waiting blocks: lane t tests 8-q
+    // sub-block t % 4 of block t / 4 against STRICT as the walks so far left
+    // it; the open sub-blocks are pushed and walked four at a time.
+    auto sub_step = [&](uint32_t c) {
+      SKC_T0(t_sub);
+      const uint32_t slot = lane >> 2;
+      const bool valid = slot < c;
+      const uint32_t sid = bq[bq_n - c + (valid ? slot : c - 1)] * 4 + (lane & 3);
+      bq_n -= c;
+      uint32_t Us = 0;
+      if (valid) {
+        const uint4 sm = smin[sid];
+#pragma unroll
+        for (int w = 0; w < NW; ++w)
+          Us |= pack_guards(ge_bytes(pH[w], word_of(sm, w))) << (4 * w);
+        Us &= NSUB - 1;
+      }
+      const bool us_strict = in_strict(Us);  // every lane (shuffle)
+      const uint32_t open = __ballot_sync(kFull, valid && !us_strict);
+      SKC_COUNT(10, c * 4);
+      SKC_COUNT(11, __popc(open));
+      if constexpr (CAP && !REG) since += 1;
+      __syncwarp();
+      if ((open >> lane) & 1u) wq[wq_n + __popc(open & lt_mask)] = sid;
+      wq_n += __popc(open);
+      __syncwarp();
+      SKC_TADD(14, t_sub);
+      while (wq_n >= 4) walk_step(4);
+    };
+
     uint32_t next_blk = 0;  // blocks below this one were already visited
     // Partitions are tested 32 at a time (lane t tests partition b0 + t):
     // a partition is skipped when the attributes its points may win on
@@ -673,8 +724,8 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
         }
         const uint32_t kb = g + __shfl_sync(kFull, base, j);
         const bool in_list = g < total;
-        // Blocks are tested against their byte-wise minimum cells, then
-        // the surviving blocks are walked one by one.
+        // Blocks are tested against their byte-wise minimum cells; the
+        // surviving ones wait for their quarters' tests (sub_step).
         uint32_t Ub = 0;
         if (in_list) {
           const uint4 bm = bmin[kb];
@@ -692,56 +743,19 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
           SKC_TADD(13, t_box);
           continue;
         }
-        // The open blocks, compacted into the warp's list (previous readers
-        // are past the fence).
-        const uint32_t nb = __popc(blocks);
+        // The open blocks go on the warp's stack (earlier readers of those
+        // entries are past the fence).
         __syncwarp();
-        if ((blocks >> lane) & 1u) wl[__popc(blocks & lt_mask)] = kb;
+        if ((blocks >> lane) & 1u) bq[bq_n + __popc(blocks & lt_mask)] = kb;
+        bq_n += __popc(blocks);
         __syncwarp();
         SKC_TADD(13, t_box);
-        for (uint32_t i0 = 0; i0 < nb; i0 += 8) {
-          SKC_T0(t_sub);
-          // Sub-box tests: lane t takes 8-q sub-block t % 4 of open block
-          // i0 + t / 4, against STRICT as the walks so far left it.
-          const uint32_t slot = i0 + (lane >> 2);
-          const bool valid = slot < nb;
-          const uint32_t sid = wl[valid ? slot : nb - 1] * 4 + (lane & 3);
-          uint32_t Us = 0;
-          if (valid) {
-            const uint4 sm = smin[sid];
-#pragma unroll
-            for (int w = 0; w < NW; ++w)
-              Us |= pack_guards(ge_bytes(pH[w], word_of(sm, w))) << (4 * w);
-            Us &= NSUB - 1;
-          }
-          const bool us_strict = in_strict(Us);  // every lane (shuffle)
-          const uint32_t open = __ballot_sync(kFull, valid && !us_strict);
-          SKC_COUNT(10, min(8u, nb - i0) * 4);
-          SKC_COUNT(11, __popc(open));
-          if constexpr (CAP && !REG) since += 1;
-          if (!open) {
-            SKC_TADD(14, t_sub);
-            continue;
-          }
-          const uint32_t no = __popc(open);
-          __syncwarp();
-          if ((open >> lane) & 1u) wo[__popc(open & lt_mask)] = sid;
-          __syncwarp();
-          SKC_TADD(14, t_sub);
-          // Walks: four open sub-blocks per step, lane t on q t % 8 of
-          // sub-block j0 + t / 8; lanes past the last one repeat it (a q
-          // tested twice changes nothing). The q arrays are padded to whole
-          // blocks with entries that add nothing (k_pad_q).
-          for (uint32_t j0 = 0; j0 < no; j0 += 4) {
-            const uint32_t jj = min(j0 + (lane >> 3), no - 1);
-            SKC_T0(t_walk);
-            test_q(wo[jj] * 8 + (lane & 7));
-            SKC_TADD(15, t_walk);
-            if constexpr (CAP && !REG) since += 1;
-          }
-        }
+        while (bq_n >= 8) sub_step(8);
       }
     }
+    // What still waits: one short sub-box step, then short walk steps.
+    if (bq_n) sub_step(bq_n);
+    while (wq_n) walk_step(min(4u, wq_n));
 
     // Output: dominated = STRICT | TIE, extended = TIE \ STRICT, with TIE
     // from the closed tie map. Bit 0 (the empty subspace) is cleared.
