@@ -818,7 +818,8 @@ def record_useful(workload):
              "block_boxes_tested", "walk_steps", "walk_steps_all_covered",
              "strict_updates", "tie_pairs", "uncovered_q_tested", "sub_boxes_tested",
              "sub_blocks_opened", "cycles_partition_ballots", "cycles_box_tests",
-             "cycles_quarter_box_tests", "cycles_walks", "cycles_candidate", "cycles_output"]
+             "cycles_quarter_and_half_box_tests", "cycles_walks", "cycles_candidate",
+             "cycles_output", "half_boxes_tested", "halves_opened"]
     useful = {"per_candidate": {nm: round(c[i] / m, 3) for i, nm in enumerate(names) if i},
               "candidates": int(c[0]),
               "useful_walk_fraction": round(1 - c[6] / max(1, c[5]), 4),

@@ -407,12 +407,13 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   SKC_TRY(A.alloc(&xq, (uint64_t)d * m_pad));
   SKC_TRY(launch_gather_soa(s, ds->x, ds->n_pad, d, F.cand, m_ptr, m, m_pad, xc));
   float* pivots;
-  uint4 *cc, *qc, *bmin, *smin;
+  uint4 *cc, *qc, *bmin, *smin, *hmin;
   SKC_TRY(A.alloc(&pivots, (uint64_t)kMaxDims * kMaxPivots));
   SKC_TRY(A.alloc(&cc, m));
   SKC_TRY(A.alloc(&qc, round_up(m, 32)));  // padded to whole blocks (k_pad_q)
   SKC_TRY(A.alloc(&bmin, (m + 31) / 32));
   SKC_TRY(A.alloc(&smin, (m + 31) / 32 * 4));
+  SKC_TRY(A.alloc(&hmin, (m + 31) / 32 * 8));
   SKC_TRY(launch_pivots_cells(s, ds->x, ds->n_pad, d, F.cand, m_ptr, m, depth, pivots, cc));
 
   // q list: the full-space skyline only. If a point q' weakly dominates q
@@ -475,7 +476,7 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   SKC_TRY(launch_gather_soa(s, ds->x, ds->n_pad, d, qids, mq_ptr, m, m_pad, xq));
   SKC_TRY(launch_gather_u4(s, cc, qidx, mq_ptr, m, qc));
   SKC_TRY(launch_pad_q(s, mq_ptr, d, qc, xq, m_pad));
-  SKC_TRY(launch_block_min(s, qc, mq_ptr, m, bmin, smin));
+  SKC_TRY(launch_block_min(s, qc, mq_ptr, m, bmin, smin, hmin));
 
   T.mark("cand: cells+q order");
   uint32_t *dom, *ext = nullptr, *work;
@@ -487,7 +488,7 @@ static int run_bitmaps(Exec& E, skc_dataset* ds, const skc_options& o,
   uint32_t* slab = nullptr;
   SKC_TRY(bitmap_tie_slab_words(d, ctx->num_sms, &slab_words));
   if (slab_words) SKC_TRY(A.alloc(&slab, slab_words));
-  BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, smin, boff, LT.unrank, K, LT.B, depth,
+  BitmapArgs ba{cc, xc, m_pad, qc, xq, bmin, smin, hmin, boff, LT.unrank, K, LT.B, depth,
                 m_ptr, work, (uint32_t)P.chunk, 0xffffffffu, dom, ext,
                 P.blocks_per_sm * ctx->num_sms, slab};
   // A cap below d - 1 lets the kernel skip q's that only reach subspaces

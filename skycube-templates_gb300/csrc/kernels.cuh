@@ -46,7 +46,7 @@ int launch_gather_soa(cudaStream_t s, const float* x, uint64_t n_pad, int d,
 int launch_gather_u4(cudaStream_t s, const uint4* in, const uint32_t* perm,
                      const uint32_t* m_ptr, uint64_t m_max, uint4* out);
 int launch_block_min(cudaStream_t s, const uint4* cells, const uint32_t* m_ptr,
-                     uint64_t m_max, uint4* bmin, uint4* smin);
+                     uint64_t m_max, uint4* bmin, uint4* smin, uint4* hmin);
 int launch_csr_gather(cudaStream_t s, const uint32_t* const* srcs,
                       const uint64_t* dst_off, uint32_t ncub, uint32_t* dst);
 int launch_set_u32(cudaStream_t s, uint32_t* p, uint32_t v);
@@ -187,6 +187,7 @@ struct BitmapArgs {
   const float* qx;       // q order, attribute-major, pitch p_pad
   const uint4* bmin;     // per block of 32 q's: byte-wise minimum cells
   const uint4* smin;     // the same per 8-q sub-block (4 per block)
+  const uint4* hmin;     // the same per 4-q half of a sub-block (8 per block)
   const uint32_t* boff;  // q partitions: offsets in q order [K + 1]
   const uint32_t* unrank;  // partition rank -> median mask over B attributes
   uint32_t K;

@@ -75,9 +75,10 @@ constexpr uint32_t kFull = 0xffffffffu;
 // q's were all covered already, [7] STRICT updates, [8] tie pairs, [9] q's
 // tested that were not covered, [10] 8-q sub-boxes tested, [11] sub-blocks
 // opened; SM cycles (clock64, per warp, summed) spent in [12] partition
-// ballots, [13] box tests, [14] quarter-box tests, [15] walks, [16] the
-// whole candidate and [17] its output.
-constexpr int kBitmapCounters = 18;
+// ballots, [13] box tests, [14] quarter- and half-box tests, [15] walks,
+// [16] the whole candidate and [17] its output; [18] 4-q half boxes tested,
+// [19] halves opened.
+constexpr int kBitmapCounters = 20;
 #if SKC_BITMAP_COUNTERS
 __device__ unsigned long long g_bitmap_counters[kBitmapCounters];
 #define SKC_COUNT(i, v) (cnt_[i] += (v))
@@ -121,10 +122,10 @@ struct BitState {
   // map is used only when a candidate has more.
   static constexpr uint32_t LIST_WORDS = A_SMEM ? 0 : 32;
   // The walk's queues, last: open blocks (up to 7 waiting + 32 from a
-  // box-test step) and open 8-q sub-blocks (up to 3 waiting + 32 from a
-  // sub-box step).
-  static constexpr uint32_t BQ_WORDS = 40, WQ_WORDS = 36;
-  static constexpr uint32_t WALK_WORDS = BQ_WORDS + WQ_WORDS;
+  // box-test step), open 8-q quarters (up to 15 + 32 from a quarter step)
+  // and open 4-q halves (up to 7 + 32 from a half step).
+  static constexpr uint32_t BQ_WORDS = 40, WQ_WORDS = 48, HQ_WORDS = 40;
+  static constexpr uint32_t WALK_WORDS = BQ_WORDS + WQ_WORDS + HQ_WORDS;
   // shared memory per warp, in words
   static constexpr uint32_t SMEM_WORDS =
       (REG ? 0 : W) + (A_SMEM ? AW : 0) + CHUNK_WORDS + LIST_WORDS + WALK_WORDS;
@@ -379,7 +380,8 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
     const uint4* __restrict__ pcells, const float* __restrict__ px,
     uint64_t p_pad, const uint4* __restrict__ qcells,
     const float* __restrict__ qx, const uint4* __restrict__ bmin,
-    const uint4* __restrict__ smin, const uint32_t* __restrict__ boff, const uint32_t* __restrict__ unrank,
+    const uint4* __restrict__ smin, const uint4* __restrict__ hmin,
+    const uint32_t* __restrict__ boff, const uint32_t* __restrict__ unrank,
     uint32_t K, int B, int depth,
     const uint32_t* __restrict__ m_ptr, uint32_t* __restrict__ work, uint32_t chunk,
     uint32_t p_end_cap, uint32_t* __restrict__ out_dom,
@@ -397,7 +399,8 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
   const int wib = threadIdx.x >> 5;
   uint32_t* wsm = smem + (size_t)wib * BS::SMEM_WORDS;
   uint32_t* bq = wsm + BS::SMEM_WORDS - BS::WALK_WORDS;  // open blocks, waiting
-  uint32_t* wq = bq + BS::BQ_WORDS;                      // open sub-blocks, waiting
+  uint32_t* wq = bq + BS::BQ_WORDS;                      // open quarters, waiting
+  uint32_t* hq = wq + BS::WQ_WORDS;                      // open halves, waiting
   const uint32_t lt_mask = (1u << lane) - 1u;
   uint32_t* sat_s = REG ? nullptr : wsm;
   uint32_t* A = BS::A_SMEM
@@ -612,28 +615,59 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
       }
     };
 
-    // Open blocks and open 8-q sub-blocks wait in per-warp stacks until a
-    // full step's worth is there (8 blocks' quarters per sub-box step, 4
-    // sub-blocks per walk step), so steps stay full across box-test steps;
-    // the order they are taken in does not matter for the result.
-    uint32_t bq_n = 0, wq_n = 0;
-    // Walk step over the top c (<= 4) waiting sub-blocks: lane t on q t % 8
-    // of sub-block t / 8; lanes past the last one repeat it (a q tested
-    // twice changes nothing). The q arrays are padded to whole blocks with
+    // Open blocks, 8-q quarters and 4-q halves wait in per-warp stacks
+    // until a full step's worth is there (8 blocks' quarters per quarter
+    // step, 16 quarters' halves per half step, 8 halves per walk step), so
+    // steps stay full across box-test steps; the order they are taken in
+    // does not matter for the result.
+    uint32_t bq_n = 0, wq_n = 0, hq_n = 0;
+    // Walk step over the top c (<= 8) waiting halves: lane t on q t % 4 of
+    // half t / 4; lanes past the last one repeat it (a q tested twice
+    // changes nothing). The q arrays are padded to whole blocks with
     // entries that add nothing (k_pad_q).
     auto walk_step = [&](uint32_t c) {
       SKC_T0(t_walk);
-      const uint32_t jj = min((uint32_t)(lane >> 3), c - 1);
-      const uint32_t qi = wq[wq_n - c + jj] * 8 + (lane & 7);
-      wq_n -= c;
+      const uint32_t jj = min((uint32_t)(lane >> 2), c - 1);
+      const uint32_t qi = hq[hq_n - c + jj] * 4 + (lane & 3);
+      hq_n -= c;
       __syncwarp();  // read before a later push overwrites the entry
       test_q(qi);
       SKC_TADD(15, t_walk);
       if constexpr (CAP && !REG) since += 1;
     };
-    // Sub-box step over the top c (<= 8) waiting blocks: lane t tests 8-q
-    // sub-block t % 4 of block t / 4 against STRICT as the walks so far left
-    // it; the open sub-blocks are pushed and walked four at a time.
+    // Half step over the top c (<= 16) waiting quarters: lane t tests 4-q
+    // half t % 2 of quarter t / 2; the open halves are pushed and walked
+    // eight at a time.
+    auto half_step = [&](uint32_t c) {
+      SKC_T0(t_half);
+      const uint32_t slot = lane >> 1;
+      const bool valid = slot < c;
+      const uint32_t hid = wq[wq_n - c + (valid ? slot : c - 1)] * 2 + (lane & 1);
+      wq_n -= c;
+      uint32_t Uh = 0;
+      if (valid) {
+        const uint4 hm = hmin[hid];
+#pragma unroll
+        for (int w = 0; w < NW; ++w)
+          Uh |= pack_guards(ge_bytes(pH[w], word_of(hm, w))) << (4 * w);
+        Uh &= NSUB - 1;
+      }
+      const bool uh_strict = in_strict(Uh);  // every lane (shuffle)
+      const uint32_t open = __ballot_sync(kFull, valid && !uh_strict);
+      SKC_COUNT(18, c * 2);
+      SKC_COUNT(19, __popc(open));
+      if constexpr (CAP && !REG) since += 1;
+      __syncwarp();
+      if ((open >> lane) & 1u) hq[hq_n + __popc(open & lt_mask)] = hid;
+      hq_n += __popc(open);
+      __syncwarp();
+      SKC_TADD(14, t_half);
+      while (hq_n >= 8) walk_step(8);
+    };
+    // Quarter step over the top c (<= 8) waiting blocks: lane t tests 8-q
+    // quarter t % 4 of block t / 4 against STRICT as the walks so far left
+    // it; the open quarters are pushed and their halves tested sixteen
+    // quarters at a time.
     auto sub_step = [&](uint32_t c) {
       SKC_T0(t_sub);
       const uint32_t slot = lane >> 2;
@@ -658,7 +692,7 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
       wq_n += __popc(open);
       __syncwarp();
       SKC_TADD(14, t_sub);
-      while (wq_n >= 4) walk_step(4);
+      while (wq_n >= 16) half_step(16);
     };
 
     uint32_t next_blk = 0;  // blocks below this one were already visited
@@ -753,9 +787,10 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
         while (bq_n >= 8) sub_step(8);
       }
     }
-    // What still waits: one short sub-box step, then short walk steps.
+    // What still waits: one short step of each kind.
     if (bq_n) sub_step(bq_n);
-    while (wq_n) walk_step(min(4u, wq_n));
+    if (wq_n) half_step(wq_n);
+    if (hq_n) walk_step(hq_n);
 
     // Output: dominated = STRICT | TIE, extended = TIE \ STRICT, with TIE
     // from the closed tie map. Bit 0 (the empty subspace) is cleared.
@@ -870,7 +905,7 @@ static int launch_bitmaps_dc(cudaStream_t s, int num_sms, const BitmapArgs& a) {
   SKC_TRY((bitmap_grid_dc<D, CAP>(num_sms, &grid, &smem)));
   if (a.grid_blocks > 0 && a.grid_blocks < grid) grid = a.grid_blocks;
   k_bitmaps<D, CAP><<<grid, 256, smem, s>>>(a.pcells, a.px, a.p_pad, a.qcells, a.qx,
-                                             a.bmin, a.smin, a.boff, a.unrank, a.K, a.B, a.depth,
+                                             a.bmin, a.smin, a.hmin, a.boff, a.unrank, a.K, a.B, a.depth,
                                              a.m_ptr, a.work, a.chunk ? a.chunk : 1u, a.p_end,
                                              a.out_dom, a.out_ext,
                                              a.tie_slab, a.cap, a.full_dom);
@@ -909,7 +944,7 @@ static int launch_bitmaps_d(cudaStream_t s, int num_sms, const BitmapArgs& a) {
   }
 
 #if SKC_BITMAP_COUNTERS
-// Counters build only: copies the kBitmapCounters (18) summed counters out
+// Counters build only: copies the kBitmapCounters (20) summed counters out
 // (`out` holds at least that many) and, when reset is nonzero, zeroes them.
 extern "C" int skc_debug_bitmap_counters(unsigned long long* out, int reset) {
   if (cudaMemcpyFromSymbol(out, g_bitmap_counters, sizeof(g_bitmap_counters)) != cudaSuccess)

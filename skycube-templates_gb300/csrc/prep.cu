@@ -433,12 +433,14 @@ __global__ void k_gather_u4(const uint4* __restrict__ in,
     out[i] = in[perm[i]];
 }
 
-// Per block of 32 consecutive q's, and per 8-q quarter of it: byte-wise
+// Per block of 32 consecutive q's, per 8-q quarter and per 4-q half of a
+// quarter: byte-wise
 // minimum of their cells. Padding entries (index >= m) get cell 127 so they
 // never lower the minimum.
 __global__ void k_block_min(const uint4* __restrict__ cells,
                             const uint32_t* __restrict__ m_ptr,
-                            uint4* __restrict__ bmin, uint4* __restrict__ smin) {
+                            uint4* __restrict__ bmin, uint4* __restrict__ smin,
+                            uint4* __restrict__ hmin) {
   const uint32_t m = *m_ptr;
   const uint32_t nblk = (m + 31) / 32;
   const int lane = threadIdx.x & 31;
@@ -451,6 +453,7 @@ __global__ void k_block_min(const uint4* __restrict__ cells,
       c.y = __vminu4(c.y, __shfl_xor_sync(0xffffffffu, c.y, o));
       c.z = __vminu4(c.z, __shfl_xor_sync(0xffffffffu, c.z, o));
       c.w = __vminu4(c.w, __shfl_xor_sync(0xffffffffu, c.w, o));
+      if (o == 2 && (lane & 3) == 0) hmin[(uint64_t)b * 8 + (lane >> 2)] = c;
       if (o == 4 && (lane & 7) == 0) smin[(uint64_t)b * 4 + (lane >> 3)] = c;
     }
     if (lane == 0) bmin[b] = c;
@@ -634,8 +637,8 @@ int launch_gather_u4(cudaStream_t s, const uint4* in, const uint32_t* perm,
 }
 
 int launch_block_min(cudaStream_t s, const uint4* cells, const uint32_t* m_ptr,
-                     uint64_t m_max, uint4* bmin, uint4* smin) {
-  k_block_min<<<grid_for(m_max, 256, 152 * 8), 256, 0, s>>>(cells, m_ptr, bmin, smin);
+                     uint64_t m_max, uint4* bmin, uint4* smin, uint4* hmin) {
+  k_block_min<<<grid_for(m_max, 256, 152 * 8), 256, 0, s>>>(cells, m_ptr, bmin, smin, hmin);
   SKC_LAUNCH_CHECK();
   return SKC_OK;
 }
