@@ -621,20 +621,26 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
     // steps stay full across box-test steps; the order they are taken in
     // does not matter for the result.
     uint32_t bq_n = 0, wq_n = 0, hq_n = 0;
-    // Walk step over the top c (<= 8) waiting halves: lane t on q t % 4 of
-    // half t / 4; lanes past the last one repeat it (a q tested twice
+    // Walk step over the top c waiting halves (c <= 8: lane t on q t % 4 of
+    // half t / 4) or, with `quarters`, quarters (c <= 4: lane t on q t % 8
+    // of quarter t / 8); lanes past the last one repeat it (a q tested twice
     // changes nothing). The q arrays are padded to whole blocks with
-    // entries that add nothing (k_pad_q).
-    auto walk_step = [&](uint32_t c) {
+    // entries that add nothing (k_pad_q). One call site of test_q: a second
+    // one spilled the capped 15-attribute kernel.
+    auto walk = [&](bool quarters, uint32_t c) {
       SKC_T0(t_walk);
-      const uint32_t jj = min((uint32_t)(lane >> 2), c - 1);
-      const uint32_t qi = hq[hq_n - c + jj] * 4 + (lane & 3);
-      hq_n -= c;
+      const int lg = quarters ? 3 : 2;  // log2 of the q's per entry
+      uint32_t* st = quarters ? wq : hq;
+      uint32_t& n = quarters ? wq_n : hq_n;
+      const uint32_t jj = min((uint32_t)lane >> lg, c - 1);
+      const uint32_t qi = (st[n - c + jj] << lg) + ((uint32_t)lane & ((1u << lg) - 1u));
+      n -= c;
       __syncwarp();  // read before a later push overwrites the entry
       test_q(qi);
       SKC_TADD(15, t_walk);
       if constexpr (CAP && !REG) since += 1;
     };
+    auto walk_step = [&](uint32_t c) { walk(false, c); };
     // Half step over the top c (<= 16) waiting quarters: lane t tests 4-q
     // half t % 2 of quarter t / 2; the open halves are pushed and walked
     // eight at a time.
@@ -787,9 +793,13 @@ __global__ void __launch_bounds__(256, (D <= 10 ? (CAP ? 6 : 8) : 4)) k_bitmaps(
         while (bq_n >= 8) sub_step(8);
       }
     }
-    // What still waits: one short step of each kind.
+    // What still waits: one short step of each kind, except that at most
+    // four waiting quarters are walked whole (one step instead of a half
+    // step and a walk step: candidates with a single open block, as on
+    // correlated data, mostly end here).
     if (bq_n) sub_step(bq_n);
-    if (wq_n) half_step(wq_n);
+    if (wq_n > 4) half_step(wq_n);
+    else if (wq_n) walk(true, wq_n);
     if (hq_n) walk_step(hq_n);
 
     // Output: dominated = STRICT | TIE, extended = TIE \ STRICT, with TIE
