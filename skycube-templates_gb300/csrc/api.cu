@@ -1013,19 +1013,34 @@ static int run_levels(Exec& E, skc_dataset* ds, const skc_options& o, int max_d,
   return jobs[0].status;
 }
 
-// The level form replaces the bitmaps for batched capped skycubes of small
-// caps on many candidates, when no per-point bitmaps are wanted and no plan
-// is being recorded (the level form syncs per level). Below 65,536
-// candidates the bitmap kernel is as fast or faster, and tie-heavy data
-// (whose small cuboids have skylines over the level kernels' capacities)
-// has few candidates.
+// The level form can replace the bitmaps for batched capped skycubes of
+// small caps, when no per-point bitmaps are wanted and no plan is being
+// recorded (the level form syncs per level). Auto takes it where it was
+// faster on one GB300 (device ms, level / bitmap form, cap 4 unless noted):
+//   16 attributes: anticorrelated 500k 48.3 / 83.5, 396k 36.7 / 64.1;
+//     uniform 937k 69.4 / 84.8, 200k 16.0 / 17.2
+//   14-15 attributes: anticorrelated 799k x 14 (737k candidates) 51.9 /
+//     58.8; but anticorrelated 150k x 14 9.7 / 9.1 and uniform 951k x 15
+//     (503k candidates) 49.2 / 39.9
+//   12 attributes and fewer, cap 4: anticorrelated 500k x 12 17.7 / 17.7,
+//     1M x 10 15.3 / 11.5
+//   caps under 4: anticorrelated 1M x 8 cap 3 4.55 / 4.69, uniform
+//     400k x 11 cap 2 2.3 / 2.8
+// Below 65,536 candidates the bitmap kernel is as fast or faster, and
+// tie-heavy data (whose small cuboids have skylines over the level kernels'
+// capacities) has few candidates.
 constexpr uint64_t kLvMinCandidates = 65536;
+constexpr uint64_t kLvMinCandidatesMidD = 600000;  // 14 and 15 attributes
+static bool levels_by_default(int d, int max_d, uint64_t candidates) {
+  if (candidates < kLvMinCandidates) return false;
+  return max_d <= 3 || d >= 16 || (d >= 14 && candidates >= kLvMinCandidatesMidD);
+}
 static bool use_levels(const Exec& E, const skc_dataset* ds, const skc_options& o, int max_d,
                        const FullSpace& F) {
   if (o.form == SKC_FORM_BITMAPS) return false;
   const bool can = !E.plan && o.mode == SKC_MODE_BATCHED && !o.want_bitmaps &&
                    max_d <= kLvMaxDims && max_d <= ds->d - 2 && ds->n < (1ull << 31);
-  return can && (o.form == SKC_FORM_LEVELS || F.h_counts[2] >= kLvMinCandidates);
+  return can && (o.form == SKC_FORM_LEVELS || levels_by_default(ds->d, max_d, F.h_counts[2]));
 }
 
 static int auto_depth(uint64_t n, int d) {

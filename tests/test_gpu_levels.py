@@ -90,6 +90,17 @@ def test_levels_duplicates_and_signed_zero(gpu_ctx):
     check(gpu_ctx, x, 3)
 
 
+def auto_form(d, max_d, candidates):
+    """The form skc_skycube picks for a batched capped skycube (the rule of
+    api.cu's use_levels): the level form from 65,536 candidates when the
+    cap is under 4, at 16 attributes, or at 14-15 attributes from 600,000
+    candidates."""
+    if candidates < 65536:
+        return "bitmaps"
+    lv = max_d <= 3 or d >= 16 or (d >= 14 and candidates >= 600000)
+    return "levels" if lv else "bitmaps"
+
+
 @pytest.mark.parametrize("kind,n,d,max_d,seed", [
     ("anticorrelated", 500000, 16, 4, 1), ("uniform", 300000, 14, 3, 2),
     ("anticorrelated", 400000, 10, 4, 93), ("correlated", 500000, 16, 4, 1),
@@ -97,18 +108,22 @@ def test_levels_duplicates_and_signed_zero(gpu_ctx):
 def test_levels_equal_bitmap_form(gpu_ctx, kind, n, d, max_d, seed):
     x = datagen.generate(kind, n, d, seed)
     ds = sk.Dataset(gpu_ctx, x)
-    a = sk.skycube(gpu_ctx, ds, max_d=max_d, want_extended=True)
+    a = sk.skycube(gpu_ctx, ds, max_d=max_d, want_extended=True, form="levels")
     b = sk.skycube(gpu_ctx, ds, max_d=max_d, want_extended=True, form="bitmaps")
+    c = sk.skycube(gpu_ctx, ds, max_d=max_d, want_extended=True)
     assert b.form()[0] == "bitmaps"
-    if a.info()["n_candidates"] >= 65536:
+    cand = b.info()["n_candidates"]
+    if cand >= 65536:
         assert a.form()[0] == "levels"
+    assert c.form()[0] == auto_form(d, max_d, cand)
     for ext in (False, True):
         sa, sb = sets(a, d, max_d, ext), sets(b, d, max_d, ext)
-        for c in sa:
-            assert np.array_equal(sa[c], sb[c]), f"cuboid {c} (extended={ext})"
+        for cub in sa:
+            assert np.array_equal(sa[cub], sb[cub]), f"cuboid {cub} (extended={ext})"
     assert a.info()["total_skyline_ids"] == b.info()["total_skyline_ids"]
-    a.close()
-    b.close()
+    assert c.info()["total_skyline_ids"] == b.info()["total_skyline_ids"]
+    for r in (a, b, c):
+        r.close()
     ds.close()
 
 
