@@ -100,7 +100,10 @@ typedef struct skc_options {
                         grab, 1..64; 0 auto (1) */
   int blocks_per_sm; /* bitmap kernel: persistent CTAs per SM, 1..32 (capped
                         by occupancy); 0 auto (the occupancy limit) */
-  int form;          /* computation of a batched skycube (SKC_FORM_*): 0 auto;
+  int form;          /* computation of a batched skycube (SKC_FORM_*): 0 auto
+                        (the level form from 65,536 candidates at caps under
+                        4, at 16 attributes, or at 14-15 attributes from
+                        600,000 candidates; else the bitmaps);
                         SKC_FORM_BITMAPS; SKC_FORM_LEVELS where it applies
                         (max_d <= 4 and <= d - 2, no per-point bitmaps; it
                         hands over to the bitmaps when too many cuboids
@@ -191,8 +194,9 @@ int skc_result_free(skc_result* res);
  * requests in flight leave of `budget` (bytes; 0: 80% of the free device
  * memory). A capped skycube request (batched form, max_d <= 4 and <= d - 2,
  * no bitmaps) takes the capped skycube requests right behind it in the
- * queue (up to 8, within the budget) into the same pass: one persistent
- * lattice launch for all of them (skc_skycube_batch). Requests whose estimate exceeds the whole budget are rejected
+ * queue (up to 8, within the budget) into the same pass (skc_skycube_batch):
+ * those the level form takes share one persistent lattice launch. Requests
+ * whose estimate exceeds the whole budget are rejected
  * with SKC_ERR_REJECTED at submission. Requests that run at the same time
  * overlap on the device. Results come back in host memory (their device
  * views are empty). Host rows passed to skc_server_submit must stay valid
