@@ -53,6 +53,8 @@ def test_bruteforce_definition_tiny():
 @pytest.mark.parametrize("kind,n,d,max_d,seed", [
     ("uniform", 5000, 7, 7, 11), ("ties", 6000, 9, 9, 12), ("correlated_q", 4000, 13, 3, 13),
     ("anticorrelated", 4000, 6, 6, 14), ("correlated", 3000, 11, 11, 15),
+    ("anticorrelated", 3000, 16, 3, 16), ("uniform", 4000, 14, 4, 17), ("ties", 5000, 12, 5, 18),
+    ("anticorrelated", 2500, 10, 10, 19),
 ])
 def test_oracle_matches_reference_live(kind, n, d, max_d, seed):
     x = datagen.generate(kind, n, d, seed)
