@@ -192,11 +192,13 @@ int skc_result_free(skc_result* res);
  * one). Submitted requests wait in FIFO order; the first one starts as soon
  * as a slot is free and its estimated device-memory footprint fits what the
  * requests in flight leave of `budget` (bytes; 0: 80% of the free device
- * memory). A capped skycube request (batched form, max_d <= 4 and <= d - 2,
- * no bitmaps) takes the capped skycube requests right behind it in the
- * queue (up to 8, within the budget) into the same pass (skc_skycube_batch):
- * those the level form takes share one persistent lattice launch. Requests
- * whose estimate exceeds the whole budget are rejected
+ * memory). A capped skycube request that the level form takes (batched
+ * form, max_d <= 4 and <= d - 2, no bitmaps; SKC_FORM_LEVELS, or the
+ * automatic rule of skc_options.form with n for the candidate count) takes
+ * such requests right behind it in the queue (up to 8, within the budget)
+ * into the same pass (skc_skycube_batch), where those the level form takes
+ * share one persistent lattice launch. Requests whose estimate exceeds the
+ * whole budget are rejected
  * with SKC_ERR_REJECTED at submission. Requests that run at the same time
  * overlap on the device. Results come back in host memory (their device
  * views are empty). Host rows passed to skc_server_submit must stay valid

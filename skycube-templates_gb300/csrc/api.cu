@@ -2349,12 +2349,17 @@ struct skc_server {
 };
 
 // Requests that may share one lattice launch: batched capped skycubes the
-// lattice form may take (max_d <= kLvMaxDims and <= d - 2, no bitmaps).
+// lattice form takes (max_d <= kLvMaxDims and <= d - 2, no bitmaps; forced,
+// or by the automatic rule with n for the candidate count, its upper
+// bound). A request bound for the bitmap form keeps a slot of its own, as
+// it would run alone inside a batch's pass anyway.
 static bool batchable(const Request& q) {
   const skc_options& o = q.opt;
   const int md = (o.max_d <= 0 || o.max_d > q.d) ? q.d : o.max_d;
-  return !o.subspace && o.mode == SKC_MODE_BATCHED && !o.want_bitmaps &&
-         o.form != SKC_FORM_BITMAPS && md <= kLvMaxDims && md <= q.d - 2;
+  if (o.subspace || o.mode != SKC_MODE_BATCHED || o.want_bitmaps ||
+      o.form == SKC_FORM_BITMAPS || md > kLvMaxDims || md > q.d - 2)
+    return false;
+  return o.form == SKC_FORM_LEVELS || levels_by_default(q.d, md, q.n);
 }
 constexpr size_t kMaxServerBatch = 8;
 
