@@ -100,14 +100,23 @@ DIGEST_CASES = ("anticorr-1m-10", "corrq-566k-15-m6", "uniform-100k-6", "ties-58
 # long here: (distribution, n, d, max_d, seed), same generator and seed.
 SCALED = {"corrq-100k-15-m6": ("correlated_q", 100_000, 15, 6, 42)}
 
+# Seeded stand-ins of the reference's published capped sweeps over 500k x 16
+# files (the benchmark's reference_sweeps), at the caps whose reference run
+# finishes here.
+SWEEPS = {
+    "sweep-anticorr-500k-16-m4": ("anticorrelated", 500_000, 16, 4, 1),
+    "sweep-corr-500k-16-m4": ("correlated", 500_000, 16, 4, 1),
+    "sweep-corr-500k-16-m10": ("correlated", 500_000, 16, 10, 1),
+}
+
 
 def write_digest(name, threads):
     """Per-cuboid digest of the reference's own STSC on one full-size
-    workload (or a SCALED stand-in): for every computed cuboid its skyline
+    workload (or a SCALED or SWEEPS stand-in): for every computed cuboid its skyline
     and extended-skyline counts and the 64-bit hashes of both ascending id
     lists, plus a hash of the generated points (so a generator that differs
     is reported as such)."""
-    kind, n, d, max_d, seed = SCALED[name] if name in SCALED else datagen.CONFIGS[name]
+    kind, n, d, max_d, seed = (SCALED.get(name) or SWEEPS.get(name) or datagen.CONFIGS[name])
     x = datagen.generate(kind, n, d, seed)
     t0 = time.time()
     res = oracle.ref_stsc(x, max_d, threads=threads)

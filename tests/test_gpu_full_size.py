@@ -76,11 +76,13 @@ def test_full_space_always_present_under_cap(gpu_ctx):
 
 DIGESTS = ["uniform-100k-6", "anticorr-1m-10", "ties-581k-10", "corrq-566k-15-m6",
            "corrq-100k-15-m6"]
+# Stand-ins of the reference's published capped sweeps (500k x 16): the two
+# batched forms only (the per-cuboid form would take minutes on their
+# 2,516-26,000 cuboids).
+SWEEP_DIGESTS = ["sweep-anticorr-500k-16-m4", "sweep-corr-500k-16-m4", "sweep-corr-500k-16-m10"]
 
 
-@pytest.mark.parametrize("form", ["mdmc/batched", "sdsc/batched", "sdsc/plain"])
-@pytest.mark.parametrize("name", DIGESTS)
-def test_full_size_digest(gpu_ctx, name, form):
+def check_digest(gpu_ctx, name, form):
     dg = load_digest(name)
     if dg is None:
         pytest.skip(f"no reference digest for {name}")
@@ -105,3 +107,15 @@ def test_full_size_digest(gpu_ctx, name, form):
     assert r.info()["total_skyline_ids"] == int(dg["sky_count"].sum())
     r.close()
     ds.close()
+
+
+@pytest.mark.parametrize("form", ["mdmc/batched", "sdsc/batched", "sdsc/plain"])
+@pytest.mark.parametrize("name", DIGESTS)
+def test_full_size_digest(gpu_ctx, name, form):
+    check_digest(gpu_ctx, name, form)
+
+
+@pytest.mark.parametrize("form", ["mdmc/batched", "sdsc/batched"])
+@pytest.mark.parametrize("name", SWEEP_DIGESTS)
+def test_sweep_digest(gpu_ctx, name, form):
+    check_digest(gpu_ctx, name, form)
