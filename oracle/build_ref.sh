@@ -15,9 +15,14 @@
 #       the include path. On x86-64, --shim writes
 #       oracle/_ref/libskycube_ref_shim.so instead, so the two builds can be
 #       compared (tests/test_oracle.py).
+#   oracle/build_ref.sh --pq [REFERENCE_ROOT]
+#       The reference's PQSkycube (ExecuteQSkycubeGLPMR, src/qskycube/) with
+#       oracle/ref_pq_driver.cpp -> oracle/_ref/libskycube_ref_pq.so: a
+#       second reference algorithm the CPU tests check skylines against
+#       (portable C++, no intrinsics).
 #   oracle/build_ref.sh --stage [REFERENCE_ROOT]
 #       (default $SKC_REFERENCE_ROOT, else /root/reference)
-#       Copies the thirteen reference files this build reads into
+#       Copies the reference files these builds read into
 #       oracle/_ref/src (git-ignored), so a host without the checkout can
 #       build them. Nothing outside oracle/_ref is written.
 set -e
@@ -26,7 +31,10 @@ OUT="$HERE/_ref"
 FILES="src/stsc/HybridCube.cpp src/stsc/HybridCube.h src/hybrid/mommyq.cpp src/hybrid/mommyq.h
 src/skycube/Hashcube.h src/skycube/NodeAuxilliary.h src/skycube/Skycube.h
 src/utilities/SubTuple.h src/utilities/common2.h src/utilities/dt_avx2.h
-src/utilities/pq_filter.h src/utilities/lattice_utilities.h src/utilities/lattice_utilities.cpp"
+src/utilities/pq_filter.h src/utilities/lattice_utilities.h src/utilities/lattice_utilities.cpp
+src/qskycube/BSkyTreeEM.cc src/qskycube/BSkyTreeEM.h src/qskycube/BSkyTreeP.cc src/qskycube/BSkyTreeP.h
+src/qskycube/Common.cc src/qskycube/Common.h src/qskycube/PivotSelection.cc src/qskycube/PivotSelection.h
+src/qskycube/QSkycube.h src/qskycube/QSkycubeG.h src/qskycube/SkyTreeUtil.cc src/qskycube/SkyTreeUtil.h"
 
 if [ "$1" = "--stage" ]; then
   REF=${2:-${SKC_REFERENCE_ROOT:-/root/reference}}
@@ -36,6 +44,25 @@ if [ "$1" = "--stage" ]; then
     cp "$REF/$f" "$OUT/src/$(dirname "$f")/"
   done
   echo "staged reference sources in $OUT/src"
+  exit 0
+fi
+
+if [ "$1" = "--pq" ]; then
+  REF=${2:-${SKC_REFERENCE_ROOT:-$OUT/src}}
+  [ -f "$REF/src/qskycube/QSkycubeG.h" ] || { echo "reference QSkycube sources not found at $REF" >&2; exit 2; }
+  CXXFLAGS="-O2 -std=c++17 -fopenmp -fPIC -w -include cstdint -include cmath -include cstring -include bitset -include cassert -I$HERE/ref_shim -I$REF/src"
+  OBJ="$OUT/obj_libskycube_ref_pq.so"
+  mkdir -p "$OBJ"
+  pids=""
+  for src in "$HERE/ref_pq_driver.cpp" "$REF"/src/qskycube/*.cc; do
+    g++ $CXXFLAGS -c "$src" -o "$OBJ/$(basename "$src" | sed 's/\.c[cp]*$//').o" &
+    pids="$pids $!"
+  done
+  rc=0
+  for p in $pids; do wait "$p" || rc=1; done
+  [ $rc = 0 ] || { echo "reference PQSkycube build failed" >&2; exit 1; }
+  g++ -shared -fopenmp -o "$OUT/libskycube_ref_pq.so" "$OBJ"/*.o
+  echo "built $OUT/libskycube_ref_pq.so"
   exit 0
 fi
 

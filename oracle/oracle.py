@@ -11,6 +11,9 @@ check or time the CUDA path; the product never imports it.
                                       intrinsics of ref_shim/ elsewhere;
                                       shim=True selects the portable build
                                       made beside the AVX one on x86-64
+  ref_pq(points, max_d, threads)      the reference's PQSkycube (its parallel
+                                      QSkycube, build_ref.sh --pq; None when
+                                      not built): skylines only, ext empty
   bruteforce_bitmaps(points)          definition-level bitmaps for tiny inputs
 
 Both STSC variants return (sky, ext): dicts {cuboid mask: sorted uint32 ids}.
@@ -25,9 +28,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libskycube_ref.so")
 REF_SHIM_LIB = os.path.join(HERE, "_ref", "libskycube_ref_shim.so")
+REF_PQ_LIB = os.path.join(HERE, "_ref", "libskycube_ref_pq.so")
 
 _lib = None
 _ref = {}
+_pq = None
 
 
 def build():
@@ -76,6 +81,28 @@ def ref_lib(shim=False):
         vp, u32, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
         _ref[shim] = _bind(L, "ref_stsc", [vp, u32, i32, i32, i32, i32, i32])
     return _ref[shim]
+
+
+def ref_pq_available():
+    return os.path.exists(REF_PQ_LIB)
+
+
+def ref_pq(points, max_d=0, threads=None):
+    """Per-cuboid skylines from the reference's PQSkycube (None when not
+    built); the extended-skyline dict is empty lists (QSkycube has none)."""
+    global _pq
+    if not ref_pq_available():
+        return None
+    if _pq is None:
+        vp, u32, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
+        _pq = _bind(ctypes.CDLL(REF_PQ_LIB), "ref_pq", [vp, u32, i32, i32, i32])
+    x = np.ascontiguousarray(points, dtype=np.float32)
+    n, d = x.shape
+    md = d if max_d <= 0 or max_d > d else max_d
+    h = _pq[0](x.ctypes.data, n, d, md, _threads(threads))
+    if not h:
+        raise ValueError(f"reference PQSkycube rejected n={n} d={d}")
+    return _collect(_pq, h, d, md)
 
 
 def build_ref(reference_root=None, shim=False):

@@ -107,3 +107,29 @@ def test_reference_portable_build_matches_avx_build(case):
     for c in a[0]:
         assert np.array_equal(a[0][c], b[0][c]), f"skyline of cuboid {c}"
         assert np.array_equal(a[1][c], b[1][c]), f"extended skyline of cuboid {c}"
+
+
+@pytest.mark.skipif(not oracle.ref_pq_available(), reason="the reference's PQSkycube is not built here")
+@pytest.mark.parametrize("case", golden_names() + ["gen:ties:20000:8:8", "gen:anticorrelated:5000:10:10",
+                                                   "gen:correlated_q:20000:14:4", "gen:uniform:5000:16:3",
+                                                   "gen:correlated:8000:12:12"])
+def test_reference_pqskycube_agrees(case):
+    """The reference's second skycube algorithm, PQSkycube (sky-tree based,
+    src/qskycube/QSkycubeG.h:223-303), gives the same skyline on every
+    cuboid as the golden fixtures (the reference's STSC) and the C oracle:
+    two independent algorithms of the suite behind one set of answers."""
+    if case.startswith("gen:"):
+        _, kind, n, d, max_d = case.split(":")
+        x = datagen.generate(kind, int(n), int(d), 31)
+        max_d = int(max_d)
+        want = oracle.stsc(x, max_d)[0]
+    else:
+        x, max_d, want, _ = load_golden(case)
+    d = x.shape[1]
+    got = oracle.ref_pq(x, max_d)[0]
+    osky = oracle.stsc(x, max_d)[0]
+    for c in range(1, 1 << d):
+        if not wanted(c, d, max_d):
+            continue
+        assert np.array_equal(got[c], want[c]), f"skyline of cuboid {c}"
+        assert np.array_equal(osky[c], want[c]), f"oracle skyline of cuboid {c}"
