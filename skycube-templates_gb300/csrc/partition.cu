@@ -536,6 +536,14 @@ __global__ void __launch_bounds__(256, (!LV && NA <= 10) ? 6 : 1) k_skyline_part
   // In strength order the boxes are loose and the test only costs
   // (1M x 10 anticorrelated: 6.9 -> 8.3 ms).
   constexpr bool box = BOX;
+  // With tile boxes a tile's floats are fetched only when some lane of the
+  // warp walks it (after the box test, so a tile every lane's box rejects is
+  // never read past its cells). Measured on anticorrelated data, full-space
+  // skyline, before -> after: 1M x 6 0.81 -> 0.77 ms, x 8 2.67 -> 2.48, x 9
+  // 4.60 -> 4.39, x 10 5.95 -> 5.83, 600k x 11 4.87 -> 4.37, 400k x 14
+  // 5.18 -> 4.80; slower at 400k x 12 (3.57 -> 3.63) and 300k x 16 (3.85
+  // -> 3.91), which load the floats with the cells as before.
+  constexpr bool defer_x = box && NA != 12 && NA != 16;
   const uint32_t wbase = threadIdx.x & ~31u;  // this warp's slice
   bool wdone = false;  // every point of the warp is settled
   for (uint32_t si = s0; si < s1 && !wdone && acc < s_hi; ++si) {
@@ -585,7 +593,9 @@ __global__ void __launch_bounds__(256, (!LV && NA <= 10) ? 6 : 1) k_skyline_part
       if (j < qend) {
         // Confirmed lists are written during this launch by other SMs: read
         // them through L2 (ld.cg), never from a possibly stale L1 line.
-        if (conf) {
+        if constexpr (defer_x) {
+          qcl = conf ? __ldcg(qc + j) : qc[j];
+        } else if (conf) {
           qcl = __ldcg(qc + j);
 #pragma unroll
           for (int k = 0; k < NA; ++k) q_x[k][threadIdx.x] = __ldcg(qxs + (uint64_t)k * a.pitch + j);
@@ -609,8 +619,20 @@ __global__ void __launch_bounds__(256, (!LV && NA <= 10) ? 6 : 1) k_skyline_part
         }
         box_out = worse != 0;
       }
+      const bool walk = !done && !(LV && beyond) && !box_out;
+      if constexpr (defer_x) {
+        if (__any_sync(kFullMask, walk) && j < qend) {
+          if (conf) {
+#pragma unroll
+            for (int k = 0; k < NA; ++k) q_x[k][threadIdx.x] = __ldcg(qxs + (uint64_t)k * a.pitch + j);
+          } else {
+#pragma unroll
+            for (int k = 0; k < NA; ++k) q_x[k][threadIdx.x] = qxs[(uint64_t)k * a.pitch + j];
+          }
+        }
+      }
       __syncwarp();
-      if (!done && !(LV && beyond) && !box_out) {
+      if (walk) {
         uint32_t lim = min(32u, qend - base);
         if (LV && !conf && sum_cut != 0xffffffffu) {
           // First q of the tile above p's level (levels ascend in a sorted
