@@ -19,12 +19,12 @@
 // of attributes where q may be <= p (LE subset of U). If U is in STRICT, the
 // down-closure of U is already strict and q adds nothing. The same test on
 // the byte-wise minimum cells of a block of 32 consecutive q's skips the
-// whole block (the box's U is the union of its q's U's), and on the minimum
-// cells of its four 8-q sub-blocks before a block is walked: on 1M x 10
-// anticorrelated, 89 % of the 32-q blocks that passed their box test held
-// no q that added anything, while 79 % of their 8-q sub-boxes were already
-// strict. q's are ordered by the lattice level of their median mask so the
-// strongest points come first and STRICT fills early.
+// whole block (the box's U is the union of its q's U's); an open block's
+// four 8-q quarters and an open quarter's two 4-q halves are box-tested the
+// same way before their q's are walked (1M x 10 anticorrelated: 89 % of the
+// 32-q blocks that passed their box test held no q that added anything,
+// while 79 % of their 8-q quarter boxes were already strict). q's are ordered
+// by the lattice level of their median mask so STRICT fills early.
 //
 // Mapping. One warp owns one p at a time (a persistent grid pulls p's from a
 // device counter) and its 32 lanes test 32 q's per step. For d <= 10 the
@@ -78,7 +78,7 @@ constexpr uint32_t kFull = 0xffffffffu;
 // ballots, [13] box tests, [14] quarter- and half-box tests, [15] walks,
 // [16] the whole candidate and [17] its output; [18] 4-q half boxes tested,
 // [19] halves opened.
-constexpr int kBitmapCounters = 20;
+[[maybe_unused]] constexpr int kBitmapCounters = 20;
 #if SKC_BITMAP_COUNTERS
 __device__ unsigned long long g_bitmap_counters[kBitmapCounters];
 #define SKC_COUNT(i, v) (cnt_[i] += (v))
