@@ -1,7 +1,8 @@
 // C entry points around the reference's PQSkycube (ExecuteQSkycubeGLPMR<D>,
-// src/qskycube/QSkycubeG.h:223-303), the suite's parallel QSkycube and the
-// second CPU algorithm its survey cross-checks STSC with. Compiled against
-// the reference sources in place by oracle/build_ref.sh --pq; the result is
+// src/qskycube/QSkycubeG.h:223-303), the suite's parallel QSkycube: a CPU
+// skycube algorithm independent of STSC (sky trees, not sort-filter
+// blocks). Compiled from the reference sources by oracle/build_ref.sh --pq
+// (staged copy or checkout); the result is
 // test infrastructure only (a second, independent check of the skylines the
 // oracle and the reference's STSC give; QSkycube has no extended skylines).
 //
