@@ -8,8 +8,10 @@ pin both the C oracle and the CUDA path on machines without the reference.
 
 Usage: python tests/golden/make_golden.py
        python tests/golden/make_golden.py --digests [workload ...]
+       python tests/golden/make_golden.py --crosscheck-pq workload ...
 The second form writes digest_<workload>.npz for the full-size benchmark
-workloads (per-cuboid counts and id-list hashes, not the id lists).
+workloads (per-cuboid counts and id-list hashes, not the id lists). The
+third checks existing digests' skylines against the reference's PQSkycube.
 """
 import hashlib
 import os
@@ -140,7 +142,35 @@ def write_digest(name, threads):
           f"{threads} threads", flush=True)
 
 
+def crosscheck_pq(name, threads):
+    """Runs the reference's PQSkycube (oracle/_ref/libskycube_ref_pq.so) on
+    a digest's workload and compares its skyline of every cuboid with the
+    digest (made by the reference's STSC): two independent reference
+    algorithms on the same full-size input. Returns the number of cuboids
+    that differ."""
+    dg = dict(np.load(os.path.join(HERE, f"digest_{name}.npz")))
+    kind, n, d, max_d, seed = (str(dg["kind"]), int(dg["n"]), int(dg["d"]), int(dg["max_d"]),
+                               int(dg["seed"]))
+    x = datagen.generate(kind, n, d, seed)
+    if points_hash(x) != int(dg["points_hash"]):
+        raise SystemExit(f"{name}: the generator gives other points than the digest's")
+    t0 = time.time()
+    res = oracle.ref_pq(x, max_d, threads=threads)
+    if res is None:
+        raise SystemExit("reference PQSkycube not built: run oracle/build_ref.sh --pq first")
+    secs = time.time() - t0
+    sky = res[0]
+    bad = [int(c) for i, c in enumerate(dg["cuboids"].tolist())
+           if len(sky[c]) != int(dg["sky_count"][i]) or id_hash(sky[c]) != int(dg["sky_hash"][i])]
+    print(f"pq-crosscheck {name}: {len(dg['cuboids'])} cuboids, {len(bad)} differ "
+          f"(first: {bad[:5]}); PQSkycube {secs:.1f} s on {threads} threads", flush=True)
+    return len(bad)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "--crosscheck-pq":
+        bad = sum(crosscheck_pq(name, os.cpu_count() or 1) for name in sys.argv[2:])
+        raise SystemExit(1 if bad else 0)
     if len(sys.argv) > 1 and sys.argv[1] == "--digests":
         names = sys.argv[2:] or DIGEST_CASES
         for name in names:

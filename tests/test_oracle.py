@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import golden_names, load_golden, wanted
+from conftest import golden_names, id_hash, load_digest, load_golden, points_hash, wanted
 from skycube_gb300 import datagen
 
 
@@ -133,3 +133,25 @@ def test_reference_pqskycube_agrees(case):
             continue
         assert np.array_equal(got[c], want[c]), f"skyline of cuboid {c}"
         assert np.array_equal(osky[c], want[c]), f"oracle skyline of cuboid {c}"
+
+
+@pytest.mark.skipif(not oracle.ref_pq_available(), reason="the reference's PQSkycube is not built here")
+@pytest.mark.parametrize("name", ["uniform-100k-6", "ties-581k-10", "corrq-100k-15-m6",
+                                  "corrq-566k-15-m6", "sweep-corr-500k-16-m4"])
+def test_full_size_digest_matches_reference_pqskycube(name):
+    """The full-size digests (made by the reference's STSC, the ones the GPU
+    forms are tested against) agree with the reference's PQSkycube on the
+    skyline of every cuboid: two independent reference algorithms at full
+    size. These workloads take PQSkycube under a second; the 1M x 10
+    anticorrelated and 500k x 16 anticorrelated -m 4 digests agree too
+    (make_golden.py --crosscheck-pq, minutes each)."""
+    dg = load_digest(name)
+    if dg is None:
+        pytest.skip(f"no digest for {name}")
+    kind, n, d, m, seed = str(dg["kind"]), int(dg["n"]), int(dg["d"]), int(dg["max_d"]), int(dg["seed"])
+    x = datagen.generate(kind, n, d, seed)
+    assert points_hash(x) == int(dg["points_hash"])
+    sky = oracle.ref_pq(x, m)[0]
+    bad = [c for i, c in enumerate(dg["cuboids"].tolist())
+           if len(sky[c]) != int(dg["sky_count"][i]) or id_hash(sky[c]) != int(dg["sky_hash"][i])]
+    assert not bad, f"{len(bad)} cuboids differ, first: {bad[:5]}"
